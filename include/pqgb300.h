@@ -1,0 +1,212 @@
+/*
+ * pqgb300 — GB300 (sm_103a) tensor-network contraction backend, C ABI.
+ *
+ * This is the drop-in boundary below PicoQuant's backend API: every function
+ * here replaces one method of the reference's `AbstractBackend` method table
+ * (src/backends.jl:3, forwarded from src/layer3.jl:124-134) or adds the
+ * plan-level executor that sits under `contract_network!` /
+ * `full_wavefunction_contraction!` (src/layer2.jl:132-195, 250-321).
+ *
+ * Conventions
+ *   - Tensors are dense, column-major (first index fastest), complex:
+ *     PQ_C64 = interleaved (re, im) float pairs (Julia ComplexF32),
+ *     PQ_C128 = interleaved (re, im) double pairs (Julia ComplexF64).
+ *   - Tensor ids are caller-chosen int64 keys (the Julia side maps each
+ *     node Symbol to an id).  A rank-0 tensor holds one element.
+ *   - Every call returns an int status: 0 = success, < 0 = error.  The
+ *     message of the last error on a context is `pq_last_error(ctx)`.
+ *     No call exits the process or traps the device; device-side failures
+ *     are reported through a status word read at the next synchronising call.
+ *   - One context = one CUDA stream on one device.  Calls on a context must
+ *     be serialised by the caller; distinct contexts are independent.
+ *   - The library owns all device memory.  Host buffers are copied on
+ *     put/get and never retained.
+ */
+#ifndef PQGB300_H
+#define PQGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PQ_OK               0
+#define PQ_ERR_INVALID     -1  /* bad argument, label/dim mismatch, bad plan   */
+#define PQ_ERR_NOT_FOUND   -2  /* unknown tensor id                             */
+#define PQ_ERR_OOM         -3  /* device allocation failed or cap exceeded      */
+#define PQ_ERR_CUDA        -4  /* CUDA runtime error                            */
+#define PQ_ERR_DEVICE      -5  /* a kernel reported failure via status word     */
+#define PQ_ERR_UNSUPPORTED -6  /* shape/precision not supported                 */
+
+/* ---- element types (host-side data) ------------------------------------ */
+#define PQ_C64   1  /* ComplexF32 */
+#define PQ_C128  2  /* ComplexF64 */
+
+/* ---- context precision modes ------------------------------------------- *
+ * PQ_PREC_C128   : tensors stored as complex128, all arithmetic FP64.
+ *                  The plain complex-FP64 CUDA path.
+ * PQ_PREC_C64    : tensors stored as complex64, FP32 arithmetic.
+ * PQ_PREC_3XTF32 : complex64 storage; large contractions run as split
+ *                  (hi+lo) TF32 tensor-core products with FP32 accumulation
+ *                  (3 products per real GEMM, 3M complex trick).
+ * PQ_PREC_3XBF16 : as 3XTF32 with bf16 hi/lo splits.                      */
+#define PQ_PREC_C128    0
+#define PQ_PREC_C64     1
+#define PQ_PREC_3XTF32  2
+#define PQ_PREC_3XBF16  3
+
+#define PQ_MAX_RANK 56
+
+typedef struct pq_ctx pq_ctx;
+typedef struct pq_plan pq_plan;
+
+/* ---- context ------------------------------------------------------------
+ * Replaces constructing `InteractiveBackend{T}()` (src/backends/interactive.jl:10-23);
+ * `precision` plays the role of the element type parameter T. */
+int pq_ctx_create(int device, int precision, pq_ctx** out);
+int pq_ctx_destroy(pq_ctx* ctx);
+const char* pq_last_error(pq_ctx* ctx);
+int pq_ctx_precision(pq_ctx* ctx);
+/* Wait for all work on the context's stream; checks the device status word. */
+int pq_ctx_sync(pq_ctx* ctx);
+/* Cap on device bytes the context may hold (0 = unlimited).  Allocations
+ * beyond the cap fail with PQ_ERR_OOM (host-side fault injection). */
+int pq_ctx_set_mem_cap(pq_ctx* ctx, int64_t bytes);
+int pq_ctx_mem_in_use(pq_ctx* ctx, int64_t* bytes);
+/* Number of kernels this context has launched so far. */
+int pq_ctx_launch_count(pq_ctx* ctx, int64_t* count);
+/* The CUDA stream of the context (a cudaStream_t), for callers that order
+ * their own work against it. */
+int pq_ctx_stream(pq_ctx* ctx, void** stream);
+
+/* ---- tensor storage ------------------------------------------------------ */
+/* src/backends/interactive.jl:32-36 `save_tensor_data` (convert(T, data)).
+ * `data` is column-major host memory of `dtype`; converted to the context's
+ * storage type on upload.  Replaces an existing tensor with the same id. */
+int pq_save_tensor_data(pq_ctx* ctx, int64_t id, int rank, const int64_t* dims,
+                        const void* data, int dtype);
+/* src/backends/interactive.jl:44-49 `load_tensor_data`.  Copies the tensor to
+ * host memory as `dtype` (dst must hold `n_elems` elements, n_elems >= size).
+ * Returns PQ_ERR_NOT_FOUND when the id is absent (the reference returns
+ * `nothing`).  Synchronises the context. */
+int pq_load_tensor_data(pq_ctx* ctx, int64_t id, void* dst, int64_t n_elems, int dtype);
+/* Rank and dims of a stored tensor (dims must hold PQ_MAX_RANK entries). */
+int pq_tensor_shape(pq_ctx* ctx, int64_t id, int* rank, int64_t* dims);
+int pq_has_tensor(pq_ctx* ctx, int64_t id);
+/* src/backends/interactive.jl:159-161 `delete_tensor!`. */
+int pq_delete_tensor(pq_ctx* ctx, int64_t id);
+/* src/backends/interactive.jl:84-88 `save_output(backend, node, name)`:
+ * the tensor `node` is also stored under `name` (a copy on the device). */
+int pq_save_output(pq_ctx* ctx, int64_t node, int64_t name);
+
+/* ---- backend tensor operations -------------------------------------------- */
+/* src/backends/interactive.jl:60-75 -> src/layer1.jl:85-92.
+ * C = tensorcontract(A, a_labels, B, b_labels, symdiff(a_labels, b_labels)):
+ * labels present in both operands are summed; C's modes are A's remaining
+ * labels in A order followed by B's remaining labels in B order.  A and B are
+ * deleted afterwards (consumed), as in the reference. */
+int pq_contract_tensors(pq_ctx* ctx, int64_t a, const int32_t* a_labels, int a_rank,
+                        int64_t b, const int32_t* b_labels, int b_rank, int64_t c);
+/* src/backends/interactive.jl:105-108 -> src/layer1.jl:111-114 (permutedims);
+ * `perm1` is 1-based, as in Julia. */
+int pq_permute_tensor(pq_ctx* ctx, int64_t id, const int32_t* perm1, int rank);
+/* src/backends/interactive.jl:97-100: reshape by index groups.  Group g holds
+ * `group_sizes[g]` consecutive 1-based axis numbers taken from `axes1`; the
+ * new dims are the products over each group (column-major, no data motion). */
+int pq_reshape_tensor(pq_ctx* ctx, int64_t id, int n_groups, const int32_t* group_sizes,
+                      const int32_t* axes1);
+/* src/backends/interactive.jl:169-172 -> src/layer1.jl:191-194 (`view_tensor!`):
+ * stores under `view_id` a copy of `node` with axis `bond_idx1` (1-based)
+ * narrowed to the 1-based inclusive range lo1:hi1. */
+int pq_view_tensor(pq_ctx* ctx, int64_t view_id, int64_t node, int bond_idx1,
+                   int64_t lo1, int64_t hi1);
+/* Gather amplitudes: out[i] = T[idx[i]] for linear (column-major) indices,
+ * written as `dtype` into host memory.  Synchronises. */
+int pq_gather_elements(pq_ctx* ctx, int64_t id, const int64_t* idx, int64_t n,
+                       void* out, int dtype);
+
+/* ---- contraction plans ----------------------------------------------------
+ * A plan is a whole pairwise contraction of a network, compiled once
+ * (mode analysis, kernel choice per pair, intermediate buffer offsets in a
+ * single arena, optional CUDA-graph capture) and executed many times.  It is
+ * the executor under `contract_network!` with a pair plan
+ * (src/layer2.jl:294-321) and under the full-wavefunction order
+ * (src/layer2.jl:132-195).
+ *
+ * Network description (host arrays):
+ *   n_leaves, leaf_ranks[n_leaves], leaf_labels[sum(ranks)] (int32 labels in
+ *   0..n_labels-1, each leaf's labels in its storage order), label_dims[n_labels].
+ *   n_steps pairs in `steps[2*i], steps[2*i+1]`: SSA operand numbers, where
+ *   0..n_leaves-1 are the leaves and n_leaves+i is the result of step i.
+ *   out_labels[n_out]: mode order of the final tensor (the last step's result).
+ * A label is summed at the first step after which no other live operand and
+ * no output still carries it (so labels shared by more than two tensors act
+ * as batch/hyper indices until their last use). */
+int pq_plan_create(pq_ctx* ctx, int n_leaves, const int32_t* leaf_ranks,
+                   const int32_t* leaf_labels, int n_labels, const int64_t* label_dims,
+                   int n_steps, const int32_t* steps, int n_out, const int32_t* out_labels,
+                   pq_plan** out);
+int pq_plan_destroy(pq_plan* plan);
+/* Cost summary of a compiled plan: complex multiply-adds (the reference's
+ * `flops` metric, src/backends.jl:37), largest intermediate (elements),
+ * arena bytes, and the number of kernel launches one execution makes. */
+int pq_plan_info(pq_plan* plan, double* cmacs, int64_t* max_elems, int64_t* arena_bytes,
+                 int64_t* launches);
+/* Execute: leaves are tensor ids already stored in the context (they are not
+ * consumed); the result is stored under `out_id`.  Asynchronous. */
+int pq_plan_execute(pq_plan* plan, const int64_t* leaf_ids, int64_t out_id);
+/* Capture one execution for `leaf_ids` into a CUDA graph; later
+ * pq_plan_execute calls with the same leaf ids replay it. */
+int pq_plan_capture(pq_plan* plan, const int64_t* leaf_ids, int64_t out_id);
+/* Per-step timing: executes once with CUDA events around every step and
+ * writes n_steps milliseconds into `ms` (used to build cost-model data). */
+int pq_plan_profile(pq_plan* plan, const int64_t* leaf_ids, int64_t out_id, float* ms);
+/* Per-step shape features: for each step, 8 doubles:
+ *   log2|A|, log2|B|, log2|C|, log2 K, log2(stride-1 run of A),
+ *   log2(stride-1 run of B), kernel class, bytes moved. */
+int pq_plan_step_features(pq_plan* plan, double* feats);
+
+/* Sliced execution.  `sliced_labels[n_sliced]` are labels of the network that
+ * are fixed to one value per slice (src/layer2/slicing.jl:37-110); all
+ * slices have identical shapes.  Slices [slice_begin, slice_end) (slice s
+ * fixes label j to digit j of s in mixed radix over the sliced dims, first
+ * label fastest) are contracted in batches of `batch` slices per launch and
+ * summed on the device with an FP64 compensated (Neumaier) sum.  The plan's
+ * output must be a scalar or small tensor; the running sum (n_out_elems
+ * complex doubles, interleaved re/im, plus the same number of compensation
+ * terms) lives on the device until `pq_sliced_result`.  Parts of the
+ * contraction tree that touch no sliced leaf are computed once per call. */
+int pq_plan_run_sliced(pq_plan* plan, const int64_t* leaf_ids, int n_sliced,
+                       const int32_t* sliced_labels, int64_t slice_begin, int64_t slice_end,
+                       int batch, int reset_sum);
+/* Copy the FP64 slice sum (interleaved re/im, n elements) to host memory. */
+int pq_sliced_result(pq_plan* plan, double* out, int64_t n);
+
+/* ---- planning ---------------------------------------------------------------
+ * Boltzmann-greedy flop-count planner, after src/layer2/bgreedy_contraction.jl:17-66:
+ * pairs are sampled with weight exp(-(cost - best)/tau) where
+ * cost = log2|C| - alpha*log2(|A|+|B|) style heuristic over pairs that share
+ * a label (then disjoint pieces by outer product); `n_trials` plans are drawn
+ * and the one with the fewest complex multiply-adds is kept.  Writes
+ * 2*(n_leaves-1) SSA operands into `steps` and returns its cost in `cmacs`
+ * and its largest intermediate in `max_elems`.  Labels in `out_labels` are
+ * kept open. */
+int pq_plan_greedy(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels,
+                   int n_labels, const int64_t* label_dims, int n_out, const int32_t* out_labels,
+                   double alpha, double tau, int n_trials, uint64_t seed,
+                   int32_t* steps, double* cmacs, int64_t* max_elems);
+/* Choose labels to slice: repeatedly fix the label that most reduces the
+ * largest intermediate (ties: least flop increase) until the largest
+ * intermediate is <= 2^log2_target elements or `max_sliced` labels are
+ * chosen.  Writes the chosen labels to `sliced` and their count to n_sliced. */
+int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels,
+                          int n_labels, const int64_t* label_dims, int n_steps,
+                          const int32_t* steps, int n_out, const int32_t* out_labels,
+                          int max_sliced, double log2_target, int32_t* sliced, int* n_sliced);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PQGB300_H */

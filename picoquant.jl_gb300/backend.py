@@ -1,0 +1,238 @@
+"""GB300Backend: the backend method table of PicoQuant over the C ABI.
+
+Mirrors the reference's `AbstractBackend` interface (src/backends.jl:3) as
+implemented by `InteractiveBackend{T}` (src/backends/interactive.jl:10-172):
+save/load/contract/save_output/reshape/permute/decompose/delete/view plus the
+`metrics` field updated by `contract_pair!` (src/layer2.jl:373).  Tensors live
+on the GPU inside the library's context; node Symbols map to int64 ids.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass
+class Metrics:
+    """src/backends.jl:8-20."""
+
+    max_tensor_size: int = 0
+    total_space_allocated: int = 0
+    flops: int = 0
+
+
+def record_compute_costs(backend, open_dims, contracted_dims):
+    """src/backends.jl:30-41: space += prod(open); flops += prod(open)*prod(contracted)."""
+    space = 1
+    for d in open_dims:
+        space *= int(d)
+    record_memory_costs(backend, space)
+    k = 1
+    for d in contracted_dims:
+        k *= int(d)
+    backend.metrics.flops += space * k
+    return space * k, space
+
+
+def record_memory_costs(backend, mem):
+    """src/backends.jl:50-57."""
+    backend.metrics.total_space_allocated += mem
+    if mem > backend.metrics.max_tensor_size:
+        backend.metrics.max_tensor_size = mem
+
+
+_PREC_NAMES = {L.PREC_C128: "c128", L.PREC_C64: "c64", L.PREC_3XTF32: "3xtf32", L.PREC_3XBF16: "3xbf16"}
+
+
+class GB300Backend:
+    """Device-resident tensor store + contraction kernels on one GB300.
+
+    ``precision`` selects storage and arithmetic (the role of the element type
+    ``T`` of ``InteractiveBackend{T}``): PREC_C128 (ComplexF64, FP64 math),
+    PREC_C64 (ComplexF32, FP32 math), PREC_3XTF32 / PREC_3XBF16 (ComplexF32
+    storage, split-precision tensor-core products for large pairs).
+    """
+
+    def __init__(self, precision: int = L.PREC_C64, device: int = 0):
+        self.lib = L.lib()
+        h = C.c_void_p()
+        rc = self.lib.pq_ctx_create(device, precision, C.byref(h))
+        if rc != L.PQ_OK:
+            raise L.PQError(rc, f"pq_ctx_create(device={device}, precision={precision}) failed")
+        self.ctx = h
+        self.precision = precision
+        self.metrics = Metrics()
+        self._ids: dict[str, int] = {}
+        self._next = 1
+
+    # ---- lifetime -----------------------------------------------------------
+    def close(self):
+        if self.ctx:
+            self.lib.pq_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def precision_name(self):
+        return _PREC_NAMES[self.precision]
+
+    def _check(self, rc, what):
+        L.check(rc, self.ctx, what)
+
+    def id_of(self, label) -> int:
+        key = str(label)
+        i = self._ids.get(key)
+        if i is None:
+            i = self._next
+            self._next += 1
+            self._ids[key] = i
+        return i
+
+    def sync(self):
+        self._check(self.lib.pq_ctx_sync(self.ctx), "sync")
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._check(self.lib.pq_ctx_launch_count(self.ctx, C.byref(v)), "launch_count")
+        return v.value
+
+    def mem_in_use(self) -> int:
+        v = C.c_int64()
+        self._check(self.lib.pq_ctx_mem_in_use(self.ctx, C.byref(v)), "mem_in_use")
+        return v.value
+
+    def set_mem_cap(self, nbytes: int):
+        self._check(self.lib.pq_ctx_set_mem_cap(self.ctx, int(nbytes)), "set_mem_cap")
+
+    # ---- backend method table ---------------------------------------------
+    def save_tensor_data(self, label, data):
+        """src/backends/interactive.jl:32-36."""
+        a = np.asarray(data)
+        if a.dtype == np.complex64:
+            a = np.asfortranarray(a)
+            dt = L.PQ_C64
+        else:
+            a = np.asfortranarray(a, dtype=np.complex128)
+            dt = L.PQ_C128
+        dims = L.arr(C.c_int64, a.shape)
+        rc = self.lib.pq_save_tensor_data(self.ctx, self.id_of(label), a.ndim, dims,
+                                          a.ctypes.data_as(C.c_void_p), dt)
+        self._check(rc, f"save_tensor_data({label})")
+
+    def has_tensor(self, label) -> bool:
+        key = str(label)
+        return key in self._ids and bool(self.lib.pq_has_tensor(self.ctx, self._ids[key]))
+
+    def shape(self, label):
+        r = C.c_int()
+        dims = (C.c_int64 * L.PQ_MAX_RANK)()
+        self._check(self.lib.pq_tensor_shape(self.ctx, self.id_of(label), C.byref(r), dims), f"shape({label})")
+        return tuple(dims[i] for i in range(r.value))
+
+    def load_tensor_data(self, label, dtype=np.complex128):
+        """src/backends/interactive.jl:44-49: the tensor as a host array, or None."""
+        if not self.has_tensor(label):
+            return None
+        shp = self.shape(label)
+        n = int(np.prod(shp)) if shp else 1
+        out = np.empty(n, dtype=dtype)
+        dt = L.PQ_C64 if np.dtype(dtype) == np.complex64 else L.PQ_C128
+        rc = self.lib.pq_load_tensor_data(self.ctx, self.id_of(label), out.ctypes.data_as(C.c_void_p), n, dt)
+        self._check(rc, f"load_tensor_data({label})")
+        if not shp:
+            return out[0]
+        return out.reshape(shp, order="F")
+
+    def contract_tensors(self, A, ia, B, ib, Cl):
+        """src/backends/interactive.jl:60-75 (A and B are consumed)."""
+        la = L.arr(C.c_int32, ia)
+        lb = L.arr(C.c_int32, ib)
+        rc = self.lib.pq_contract_tensors(self.ctx, self.id_of(A), la, len(ia), self.id_of(B), lb, len(ib),
+                                          self.id_of(Cl))
+        self._check(rc, f"contract_tensors({A}, {B} -> {Cl})")
+
+    def save_output(self, node, name="result"):
+        """src/backends/interactive.jl:84-88."""
+        self._check(self.lib.pq_save_output(self.ctx, self.id_of(node), self.id_of(name)), "save_output")
+
+    def reshape_tensor(self, tensor, groups):
+        """src/backends/interactive.jl:97-100 (groups of 1-based axes)."""
+        sizes = [len(g) for g in groups]
+        axes = [int(x) for g in groups for x in g]
+        rc = self.lib.pq_reshape_tensor(self.ctx, self.id_of(tensor), len(groups), L.arr(C.c_int32, sizes),
+                                        L.arr(C.c_int32, axes))
+        self._check(rc, f"reshape_tensor({tensor})")
+
+    def permute_tensor(self, tensor, axes):
+        """src/backends/interactive.jl:105-108 (1-based permutation)."""
+        rc = self.lib.pq_permute_tensor(self.ctx, self.id_of(tensor), L.arr(C.c_int32, axes), len(axes))
+        self._check(rc, f"permute_tensor({tensor})")
+
+    def delete_tensor(self, tensor):
+        """src/backends/interactive.jl:159-161."""
+        if str(tensor) in self._ids:
+            self._check(self.lib.pq_delete_tensor(self.ctx, self._ids[str(tensor)]), "delete_tensor")
+
+    def view_tensor(self, view_node, node, bond_idx, bond_range):
+        """src/backends/interactive.jl:169-172; bond_range is a 1-based
+        inclusive (lo, hi) pair or a ``range`` of 1-based values."""
+        if isinstance(bond_range, range):
+            lo, hi = bond_range.start, bond_range.stop - 1
+        else:
+            lo, hi = bond_range
+        rc = self.lib.pq_view_tensor(self.ctx, self.id_of(view_node), self.id_of(node), int(bond_idx), int(lo),
+                                     int(hi))
+        self._check(rc, f"view_tensor({node})")
+
+    def decompose_tensor(self, tensor, left_positions, right_positions, threshold=1e-13, max_rank=0,
+                         left_label=None, right_label=None):
+        """src/backends/interactive.jl:124-151 -> src/layer1.jl:146-184.
+
+        The SVD split is not on the contraction path; it runs on the host in
+        FP64 and the two factors are uploaded.  Returns the new bond extent.
+        """
+        data = self.load_tensor_data(tensor)
+        B, Cm, chi = decompose_array(data, left_positions, right_positions, threshold, max_rank,
+                                     eps_dtype=np.float32 if self.precision != L.PREC_C128 else np.float64)
+        self.save_tensor_data(left_label, B)
+        self.save_tensor_data(right_label, Cm)
+        self.delete_tensor(tensor)
+        return chi
+
+    # ---- bulk helpers -------------------------------------------------------
+    def gather(self, label, linear_indices, dtype=np.complex128):
+        idx = np.ascontiguousarray(linear_indices, dtype=np.int64)
+        out = np.empty(idx.size, dtype=dtype)
+        dt = L.PQ_C64 if np.dtype(dtype) == np.complex64 else L.PQ_C128
+        rc = self.lib.pq_gather_elements(self.ctx, self.id_of(label), idx.ctypes.data_as(L.i64p), idx.size,
+                                         out.ctypes.data_as(C.c_void_p), dt)
+        self._check(rc, "gather")
+        return out
+
+
+def decompose_array(tensor, left_positions, right_positions, threshold=1e-13, max_rank=0, eps_dtype=np.float64):
+    """src/layer1.jl:146-184: SVD across (left | right) positions (1-based)."""
+    dims = tensor.shape
+    ld = [dims[x - 1] for x in left_positions]
+    rd = [dims[x - 1] for x in right_positions]
+    A = np.transpose(tensor, [x - 1 for x in list(left_positions) + list(right_positions)])
+    A = np.reshape(A, (int(np.prod(ld)), int(np.prod(rd))), order="F")
+    U, S, Vh = np.linalg.svd(A, full_matrices=False)
+    threshold = max(threshold, float(np.sqrt(np.finfo(eps_dtype).eps)))
+    s_norm = float(np.sqrt(np.sum(S**2)))
+    chi = int(np.sum(S / s_norm > threshold)) if s_norm > 0 else 0
+    if max_rank > 0:
+        chi = min(max_rank, chi)
+    sq = np.sqrt(S[:chi])
+    B = np.reshape(U[:, :chi] * sq[None, :], tuple(ld) + (chi,), order="F")
+    Cm = np.reshape(sq[:, None] * Vh[:chi, :], (chi,) + tuple(rd), order="F")
+    return B, Cm, chi

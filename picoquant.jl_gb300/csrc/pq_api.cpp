@@ -1,0 +1,512 @@
+// C ABI: context, tensor table and the backend tensor operations.
+//
+// Mirrors the method table of the reference's InteractiveBackend
+// (src/backends/interactive.jl:10-172) with device-resident tensors.
+#include <algorithm>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "pq_internal.h"
+
+namespace pq {
+
+int fail(Ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+int cuda_fail(Ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  if (e == cudaErrorMemoryAllocation) return fail(ctx, PQ_ERR_OOM, m);
+  return fail(ctx, PQ_ERR_CUDA, m);
+}
+
+int dev_alloc(Ctx* ctx, size_t bytes, void** p) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (ctx->mem_cap > 0 && ctx->mem_in_use + (int64_t)bytes > ctx->mem_cap)
+    return fail(ctx, PQ_ERR_OOM,
+                "device memory cap exceeded: requested " + std::to_string(bytes) + " bytes with " +
+                    std::to_string(ctx->mem_in_use) + " of " + std::to_string(ctx->mem_cap) + " in use");
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(ctx, e, "cudaMallocFromPoolAsync");
+  }
+  ctx->mem_in_use += (int64_t)bytes;
+  return PQ_OK;
+}
+
+void dev_free(Ctx* ctx, void* p, size_t bytes) {
+  if (!p) return;
+  if (bytes == 0) bytes = 16;
+  cudaFreeAsync(p, ctx->stream);
+  ctx->mem_in_use -= (int64_t)bytes;
+}
+
+static int64_t prod(const std::vector<int64_t>& d) {
+  int64_t p = 1;
+  for (auto x : d) p *= x;
+  return p;
+}
+
+static void free_tensor(Ctx* ctx, Tensor& t) {
+  dev_free(ctx, t.ptr, t.bytes);
+  t.ptr = nullptr;
+}
+
+// Replace (or insert) a tensor entry, freeing the previous storage.
+static void put_entry(Ctx* ctx, int64_t id, Tensor&& t) {
+  auto it = ctx->tensors.find(id);
+  if (it != ctx->tensors.end()) {
+    if (it->second.ptr != t.ptr) free_tensor(ctx, it->second);
+    it->second = std::move(t);
+  } else {
+    ctx->tensors.emplace(id, std::move(t));
+  }
+}
+
+int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, Tensor& t) {
+  t.dims = dims;
+  t.size = prod(dims);
+  t.bytes = (size_t)t.size * ctx->elem;
+  return dev_alloc(ctx, t.bytes, &t.ptr);
+}
+
+int check_status(Ctx* ctx) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+  if (h != 0) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+    return fail(ctx, PQ_ERR_DEVICE, "a kernel reported device status " + std::to_string(h));
+  }
+  return PQ_OK;
+}
+
+}  // namespace pq
+
+using namespace pq;
+
+#define CTX_OR_FAIL(c)              \
+  if (!(c)) return PQ_ERR_INVALID; \
+  Ctx* ctx = &(c)->impl;
+
+extern "C" {
+
+int pq_ctx_create(int device, int precision, pq_ctx** out) {
+  if (!out) return PQ_ERR_INVALID;
+  *out = nullptr;
+  if (precision < PQ_PREC_C128 || precision > PQ_PREC_3XBF16) return PQ_ERR_INVALID;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return PQ_ERR_CUDA;
+  pq_ctx* c = new pq_ctx();
+  Ctx* ctx = &c->impl;
+  ctx->device = device;
+  ctx->precision = precision;
+  ctx->elem = precision == PQ_PREC_C128 ? 16 : 8;
+  e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return PQ_ERR_CUDA;
+  }
+  // A private stream-ordered pool that keeps freed blocks for reuse.
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  e = cudaMemPoolCreate(&ctx->pool, &props);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete c;
+    return PQ_ERR_CUDA;
+  }
+  uint64_t thr = UINT64_MAX;
+  cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  e = cudaMalloc((void**)&ctx->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    cudaMemPoolDestroy(ctx->pool);
+    cudaStreamDestroy(ctx->stream);
+    delete c;
+    return PQ_ERR_CUDA;
+  }
+  *out = c;
+  return PQ_OK;
+}
+
+int pq_ctx_destroy(pq_ctx* c) {
+  if (!c) return PQ_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  cudaSetDevice(ctx->device);
+  for (auto& kv : ctx->tensors) free_tensor(ctx, kv.second);
+  ctx->tensors.clear();
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_status);
+  cudaMemPoolDestroy(ctx->pool);
+  cudaStreamDestroy(ctx->stream);
+  delete c;
+  return PQ_OK;
+}
+
+const char* pq_last_error(pq_ctx* c) {
+  if (!c) return "null context";
+  return c->impl.last_error.c_str();
+}
+
+int pq_ctx_precision(pq_ctx* c) {
+  CTX_OR_FAIL(c);
+  return ctx->precision;
+}
+
+int pq_ctx_sync(pq_ctx* c) {
+  CTX_OR_FAIL(c);
+  return check_status(ctx);
+}
+
+int pq_ctx_set_mem_cap(pq_ctx* c, int64_t bytes) {
+  CTX_OR_FAIL(c);
+  ctx->mem_cap = bytes < 0 ? 0 : bytes;
+  return PQ_OK;
+}
+
+int pq_ctx_mem_in_use(pq_ctx* c, int64_t* bytes) {
+  CTX_OR_FAIL(c);
+  if (bytes) *bytes = ctx->mem_in_use;
+  return PQ_OK;
+}
+
+int pq_ctx_launch_count(pq_ctx* c, int64_t* count) {
+  CTX_OR_FAIL(c);
+  if (count) *count = ctx->launches;
+  return PQ_OK;
+}
+
+int pq_ctx_stream(pq_ctx* c, void** stream) {
+  CTX_OR_FAIL(c);
+  if (stream) *stream = (void*)ctx->stream;
+  return PQ_OK;
+}
+
+int pq_save_tensor_data(pq_ctx* c, int64_t id, int rank, const int64_t* dims, const void* data, int dtype) {
+  CTX_OR_FAIL(c);
+  if (rank < 0 || rank > PQ_MAX_RANK || (rank > 0 && !dims) || !data)
+    return fail(ctx, PQ_ERR_INVALID, "save_tensor_data: bad rank/dims/data");
+  if (dtype != PQ_C64 && dtype != PQ_C128) return fail(ctx, PQ_ERR_INVALID, "save_tensor_data: bad dtype");
+  std::vector<int64_t> d(dims, dims + rank);
+  for (auto x : d)
+    if (x < 1) return fail(ctx, PQ_ERR_INVALID, "save_tensor_data: extents must be >= 1");
+  Tensor t;
+  int st = alloc_tensor(ctx, d, t);
+  if (st) return st;
+  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
+  cudaError_t e;
+  if (host_elem == ctx->elem) {
+    e = cudaMemcpyAsync(t.ptr, data, t.bytes, cudaMemcpyHostToDevice, ctx->stream);
+  } else {
+    // convert on the host (gate tensors are small; large states should be
+    // uploaded in the storage type)
+    std::vector<unsigned char> tmp(t.bytes);
+    if (dtype == PQ_C128) {
+      const double* s = (const double*)data;
+      float* o = (float*)tmp.data();
+      for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (float)s[i];
+    } else {
+      const float* s = (const float*)data;
+      double* o = (double*)tmp.data();
+      for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (double)s[i];
+    }
+    e = cudaMemcpyAsync(t.ptr, tmp.data(), t.bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  }
+  if (e != cudaSuccess) {
+    free_tensor(ctx, t);
+    return cuda_fail(ctx, e, "save_tensor_data upload");
+  }
+  put_entry(ctx, id, std::move(t));
+  return PQ_OK;
+}
+
+int pq_load_tensor_data(pq_ctx* c, int64_t id, void* dst, int64_t n_elems, int dtype) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "load_tensor_data: no tensor " + std::to_string(id));
+  const Tensor& t = it->second;
+  if (!dst || n_elems < t.size) return fail(ctx, PQ_ERR_INVALID, "load_tensor_data: destination too small");
+  if (dtype != PQ_C64 && dtype != PQ_C128) return fail(ctx, PQ_ERR_INVALID, "load_tensor_data: bad dtype");
+  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
+  cudaError_t e;
+  if (host_elem == ctx->elem) {
+    e = cudaMemcpyAsync(dst, t.ptr, t.bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "load_tensor_data download");
+    return check_status(ctx);
+  }
+  std::vector<unsigned char> tmp(t.bytes);
+  e = cudaMemcpyAsync(tmp.data(), t.ptr, t.bytes, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "load_tensor_data download");
+  int st = check_status(ctx);
+  if (st) return st;
+  if (ctx->elem == 8) {
+    const float* s = (const float*)tmp.data();
+    double* o = (double*)dst;
+    for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = s[i];
+  } else {
+    const double* s = (const double*)tmp.data();
+    float* o = (float*)dst;
+    for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (float)s[i];
+  }
+  return PQ_OK;
+}
+
+int pq_tensor_shape(pq_ctx* c, int64_t id, int* rank, int64_t* dims) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "tensor_shape: no tensor " + std::to_string(id));
+  if (rank) *rank = (int)it->second.dims.size();
+  if (dims)
+    for (size_t i = 0; i < it->second.dims.size(); ++i) dims[i] = it->second.dims[i];
+  return PQ_OK;
+}
+
+int pq_has_tensor(pq_ctx* c, int64_t id) {
+  if (!c) return 0;
+  return c->impl.tensors.count(id) ? 1 : 0;
+}
+
+int pq_delete_tensor(pq_ctx* c, int64_t id) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return PQ_OK;  // deleting a missing tensor is a no-op
+  free_tensor(ctx, it->second);
+  ctx->tensors.erase(it);
+  return PQ_OK;
+}
+
+int pq_save_output(pq_ctx* c, int64_t node, int64_t name) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(node);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "save_output: no tensor " + std::to_string(node));
+  if (node == name) return PQ_OK;
+  Tensor t;
+  int st = alloc_tensor(ctx, it->second.dims, t);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(t.ptr, it->second.ptr, t.bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) {
+    free_tensor(ctx, t);
+    return cuda_fail(ctx, e, "save_output copy");
+  }
+  put_entry(ctx, name, std::move(t));
+  return PQ_OK;
+}
+
+int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_rank, int64_t b,
+                        const int32_t* b_labels, int b_rank, int64_t cid) {
+  CTX_OR_FAIL(c);
+  auto ia = ctx->tensors.find(a), ib = ctx->tensors.find(b);
+  if (ia == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "contract_tensors: no tensor " + std::to_string(a));
+  if (ib == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "contract_tensors: no tensor " + std::to_string(b));
+  if (a == b) return fail(ctx, PQ_ERR_INVALID, "contract_tensors: A and B are the same tensor");
+  Tensor& A = ia->second;
+  Tensor& B = ib->second;
+  if ((int)A.dims.size() != a_rank || (int)B.dims.size() != b_rank || (a_rank && !a_labels) ||
+      (b_rank && !b_labels))
+    return fail(ctx, PQ_ERR_INVALID, "contract_tensors: label count does not match tensor rank");
+  std::vector<int> la(a_labels, a_labels + a_rank), lb(b_labels, b_labels + b_rank);
+  std::vector<int> lc = symdiff_labels(la, lb);
+  PairPlan pp;
+  std::string err;
+  if (!analyse_pair(la, A.dims, lb, B.dims, lc, ctx->precision, pp, err))
+    return fail(ctx, PQ_ERR_INVALID, "contract_tensors: " + err);
+  Tensor C;
+  int st = alloc_tensor(ctx, pp.c_dims, C);
+  if (st) return st;
+  cudaError_t e;
+  void* scratch = nullptr;
+  size_t sbytes = 0;
+  if (pp.kclass == KC_TC) {
+    sbytes = tc_scratch_bytes(ctx->precision, pp.m);
+    st = dev_alloc(ctx, sbytes, &scratch);
+    if (st) {
+      free_tensor(ctx, C);
+      return st;
+    }
+    e = launch_tc(ctx->precision, A.ptr, B.ptr, C.ptr, pp.m, scratch, sbytes, ctx->stream);
+    ctx->launches += 4;
+  } else if (pp.kclass == KC_GEMM) {
+    e = launch_gemm(ctx->precision, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
+    ctx->launches += 1;
+  } else {
+    e = launch_generic(ctx->precision, A.ptr, B.ptr, C.ptr, pp.g, ctx->stream);
+    ctx->launches += 1;
+  }
+  if (scratch) dev_free(ctx, scratch, sbytes);
+  if (e != cudaSuccess) {
+    free_tensor(ctx, C);
+    return cuda_fail(ctx, e, "contract_tensors launch");
+  }
+  // A and B are consumed (src/backends/interactive.jl:73-74)
+  free_tensor(ctx, A);
+  free_tensor(ctx, B);
+  ctx->tensors.erase(a);
+  ctx->tensors.erase(b);
+  put_entry(ctx, cid, std::move(C));
+  return PQ_OK;
+}
+
+int pq_permute_tensor(pq_ctx* c, int64_t id, const int32_t* perm1, int rank) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "permute_tensor: no tensor " + std::to_string(id));
+  Tensor& T = it->second;
+  if ((int)T.dims.size() != rank || (rank && !perm1))
+    return fail(ctx, PQ_ERR_INVALID, "permute_tensor: permutation length does not match rank");
+  std::vector<int> seen(rank, 0);
+  for (int i = 0; i < rank; ++i) {
+    int p = perm1[i] - 1;
+    if (p < 0 || p >= rank || seen[p]) return fail(ctx, PQ_ERR_INVALID, "permute_tensor: not a permutation");
+    seen[p] = 1;
+  }
+  // a permutation is a contraction with nothing: result label i = input label perm[i]
+  std::vector<int> la(rank), lc(rank);
+  for (int i = 0; i < rank; ++i) la[i] = i;
+  for (int i = 0; i < rank; ++i) lc[i] = perm1[i] - 1;
+  PairPlan pp;
+  std::string err;
+  if (!analyse_pair(la, T.dims, {}, {}, lc, ctx->precision, pp, err))
+    return fail(ctx, PQ_ERR_INVALID, "permute_tensor: " + err);
+  Tensor O;
+  int st = alloc_tensor(ctx, pp.c_dims, O);
+  if (st) return st;
+  cudaError_t e = launch_permute(ctx->precision, T.ptr, 0, O.ptr, pp.g, ctx->stream);
+  ctx->launches += 1;
+  if (e != cudaSuccess) {
+    free_tensor(ctx, O);
+    return cuda_fail(ctx, e, "permute launch");
+  }
+  put_entry(ctx, id, std::move(O));
+  return PQ_OK;
+}
+
+int pq_reshape_tensor(pq_ctx* c, int64_t id, int n_groups, const int32_t* group_sizes, const int32_t* axes1) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "reshape_tensor: no tensor " + std::to_string(id));
+  Tensor& T = it->second;
+  if (n_groups < 0 || n_groups > PQ_MAX_RANK || (n_groups && (!group_sizes || !axes1)))
+    return fail(ctx, PQ_ERR_INVALID, "reshape_tensor: bad groups");
+  std::vector<int64_t> nd;
+  int pos = 0;
+  const int r = (int)T.dims.size();
+  for (int g = 0; g < n_groups; ++g) {
+    int64_t p = 1;
+    for (int j = 0; j < group_sizes[g]; ++j) {
+      int ax = axes1[pos++] - 1;
+      if (ax < 0 || ax >= r) return fail(ctx, PQ_ERR_INVALID, "reshape_tensor: axis out of range");
+      p *= T.dims[ax];
+    }
+    nd.push_back(p);
+  }
+  if (prod(nd) != T.size) return fail(ctx, PQ_ERR_INVALID, "reshape_tensor: size changes");
+  T.dims = nd;
+  return PQ_OK;
+}
+
+int pq_view_tensor(pq_ctx* c, int64_t view_id, int64_t node, int bond_idx1, int64_t lo1, int64_t hi1) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(node);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "view_tensor: no tensor " + std::to_string(node));
+  Tensor& T = it->second;
+  const int r = (int)T.dims.size();
+  const int ax = bond_idx1 - 1;
+  if (ax < 0 || ax >= r || lo1 < 1 || hi1 < lo1 || hi1 > T.dims[ax])
+    return fail(ctx, PQ_ERR_INVALID, "view_tensor: bad bond index or range");
+  std::vector<int> la(r);
+  for (int i = 0; i < r; ++i) la[i] = i;
+  PairPlan pp;
+  std::string err;
+  std::vector<int64_t> vd = T.dims;
+  vd[ax] = hi1 - lo1 + 1;
+  // analyse as a permutation of a tensor with the narrowed extent (the input
+  // strides are those of the full tensor)
+  if (!analyse_pair(la, T.dims, {}, {}, la, ctx->precision, pp, err))
+    return fail(ctx, PQ_ERR_INVALID, "view_tensor: " + err);
+  // rebuild the descriptor without merging across the narrowed mode
+  GenericDesc g;
+  std::memset(&g, 0, sizeof(g));
+  int64_t stride = 1, size = 1;
+  g.pow2 = 0;
+  for (int i = 0; i < r; ++i) {
+    g.cdim[g.nc] = vd[i];
+    g.csa[g.nc] = stride;
+    g.csb[g.nc] = 0;
+    g.clog[g.nc] = -1;
+    stride *= T.dims[i];
+    size *= vd[i];
+    if (vd[i] > 1) ++g.nc;
+  }
+  g.csize = size;
+  g.ksize = 1;
+  int64_t base = (lo1 - 1);
+  for (int i = 0; i < ax; ++i) base *= T.dims[i];
+  Tensor O;
+  int st = alloc_tensor(ctx, vd, O);
+  if (st) return st;
+  cudaError_t e = launch_permute(ctx->precision, T.ptr, base, O.ptr, g, ctx->stream);
+  ctx->launches += 1;
+  if (e != cudaSuccess) {
+    free_tensor(ctx, O);
+    return cuda_fail(ctx, e, "view launch");
+  }
+  put_entry(ctx, view_id, std::move(O));
+  return PQ_OK;
+}
+
+int pq_gather_elements(pq_ctx* c, int64_t id, const int64_t* idx, int64_t n, void* out, int dtype) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "gather_elements: no tensor " + std::to_string(id));
+  if (n < 0 || (n && (!idx || !out))) return fail(ctx, PQ_ERR_INVALID, "gather_elements: bad arguments");
+  if (dtype != PQ_C64 && dtype != PQ_C128) return fail(ctx, PQ_ERR_INVALID, "gather_elements: bad dtype");
+  const Tensor& T = it->second;
+  for (int64_t i = 0; i < n; ++i)
+    if (idx[i] < 0 || idx[i] >= T.size) return fail(ctx, PQ_ERR_INVALID, "gather_elements: index out of range");
+  if (n == 0) return PQ_OK;
+  void* d_idx = nullptr;
+  void* d_out = nullptr;
+  int st = dev_alloc(ctx, (size_t)n * 8, &d_idx);
+  if (st) return st;
+  st = dev_alloc(ctx, (size_t)n * ctx->elem, &d_out);
+  if (st) {
+    dev_free(ctx, d_idx, (size_t)n * 8);
+    return st;
+  }
+  cudaError_t e = cudaMemcpyAsync(d_idx, idx, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = launch_gather(ctx->precision, T.ptr, (const int64_t*)d_idx, n, d_out, ctx->stream);
+  ctx->launches += 1;
+  std::vector<unsigned char> tmp((size_t)n * ctx->elem);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d_out, tmp.size(), cudaMemcpyDeviceToHost, ctx->stream);
+  dev_free(ctx, d_idx, (size_t)n * 8);
+  dev_free(ctx, d_out, (size_t)n * ctx->elem);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gather_elements");
+  st = check_status(ctx);
+  if (st) return st;
+  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
+  if (host_elem == ctx->elem) {
+    std::memcpy(out, tmp.data(), tmp.size());
+  } else if (ctx->elem == 8) {
+    const float* s = (const float*)tmp.data();
+    double* o = (double*)out;
+    for (int64_t i = 0; i < 2 * n; ++i) o[i] = s[i];
+  } else {
+    const double* s = (const double*)tmp.data();
+    float* o = (float*)out;
+    for (int64_t i = 0; i < 2 * n; ++i) o[i] = (float)s[i];
+  }
+  return PQ_OK;
+}
+
+}  // extern "C"

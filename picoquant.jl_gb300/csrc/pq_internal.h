@@ -1,0 +1,138 @@
+// Internal declarations shared by the pqgb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/pqgb300.h"
+
+namespace pq {
+
+constexpr int kMaxModes = 32;   // modes of one side of a pair after merging
+constexpr int kGenericKTab = 2048;  // K <= this runs in the table-driven SIMT kernel
+
+// One operand / result mode after analysis: its extent and its strides (in
+// elements) in A, B and C.  A stride of 0 means the mode is absent there.
+struct Mode {
+  int64_t dim;
+  int64_t sa, sb, sc;
+};
+
+// Kernel-facing description of one pairwise contraction
+//   C[c] = sum_k A[oa(c) + ka(k)] * B[ob(c) + kb(k)]
+// where c runs over the C modes in C storage order (column-major).
+struct GenericDesc {
+  int nc;            // number of (merged) C modes
+  int nk;            // number of (merged) contracted modes
+  int pow2;          // 1 if every C and K dim is a power of two
+  int pad_;
+  int64_t csize, ksize;
+  int64_t cdim[kMaxModes], csa[kMaxModes], csb[kMaxModes];
+  int32_t clog[kMaxModes];
+  int64_t kdim[kMaxModes], ksa[kMaxModes], ksb[kMaxModes];
+  int32_t klog[kMaxModes];
+};
+
+// Description for the tiled GEMM-class kernel:
+//   C[cm(m)+cn(n)+cb(z)] = sum_k A[am(m)+ak(k)+ab(z)] * B[bk(k)+bn(n)+bb(z)]
+struct GemmDesc {
+  int64_t M, N, K, Z;
+  int nm, nn, nk, nz;
+  int64_t mdim[kMaxModes], msa[kMaxModes], msc[kMaxModes];
+  int64_t ndim[kMaxModes], nsb[kMaxModes], nsc[kMaxModes];
+  int64_t kdim[kMaxModes], ksa[kMaxModes], ksb[kMaxModes];
+  int64_t zdim[kMaxModes], zsa[kMaxModes], zsb[kMaxModes], zsc[kMaxModes];
+};
+
+enum KernelClass : int { KC_GENERIC = 0, KC_GEMM = 1, KC_TC = 2, KC_COPY = 3 };
+
+// Host-side analysis of one contraction.
+struct PairPlan {
+  std::vector<int> c_labels;   // result labels in storage order
+  std::vector<int64_t> c_dims;
+  int64_t csize = 1, ksize = 1, asize = 1, bsize = 1;
+  int64_t M = 1, N = 1, Z = 1;
+  KernelClass kclass = KC_GENERIC;
+  GenericDesc g;
+  GemmDesc m;
+  int64_t run_a = 1, run_b = 1;   // extent of the unit-stride run of A / B that
+                                   // is read contiguously (coalescing feature)
+};
+
+// Analyse C = A x B given labels (A/B storage order) and the result labels
+// (storage order).  Labels of A or B absent from C are summed.  Returns
+// false with `err` set on inconsistent input.
+bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
+                  const std::vector<int>& lb, const std::vector<int64_t>& db,
+                  const std::vector<int>& lc, int precision, PairPlan& out, std::string& err);
+
+// Result labels in the reference's order: A's labels not in B (A order),
+// then B's labels not in A (B order).
+std::vector<int> symdiff_labels(const std::vector<int>& la, const std::vector<int>& lb);
+
+struct Tensor {
+  void* ptr = nullptr;
+  std::vector<int64_t> dims;
+  int64_t size = 1;
+  size_t bytes = 0;
+};
+
+struct Ctx {
+  int device = 0;
+  int precision = PQ_PREC_C128;
+  size_t elem = 16;   // bytes per stored element
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;
+  int* d_status = nullptr;          // device status word (0 = ok)
+  std::unordered_map<int64_t, Tensor> tensors;
+  std::string last_error;
+  int64_t mem_cap = 0;
+  int64_t mem_in_use = 0;
+  int64_t launches = 0;
+};
+
+// Status helpers: set the context error and return the code.
+int fail(Ctx* ctx, int code, const std::string& msg);
+int cuda_fail(Ctx* ctx, cudaError_t e, const char* what);
+
+// Stream-ordered device allocation accounted against the context cap.
+int dev_alloc(Ctx* ctx, size_t bytes, void** p);
+void dev_free(Ctx* ctx, void* p, size_t bytes);
+
+// ---- kernel launchers (pq_kernels.cu) ----------------------------------
+// All launches are asynchronous on `stream` and return the launch error.
+cudaError_t launch_generic(int precision, const void* A, const void* B, void* C,
+                           const GenericDesc& d, cudaStream_t stream);
+cudaError_t launch_gemm(int precision, const void* A, const void* B, void* C,
+                        const GemmDesc& d, cudaStream_t stream);
+// out[c] = in[base + sum_i idx_i * stride_i] over `d` (uses csa as input
+// strides, C storage column-major).
+cudaError_t launch_permute(int precision, const void* in, int64_t base, void* out,
+                           const GenericDesc& d, cudaStream_t stream);
+cudaError_t launch_gather(int precision, const void* in, const int64_t* d_idx, int64_t n,
+                          void* out, cudaStream_t stream);
+// Batched leaf gather for slicing: out[x + xs*b] = in[x_off(x) + slice_off(s0+b)]
+// for b < nb, where x runs over `d` (csa = input strides of the kept modes)
+// and the slice offset is the mixed-radix digits of (s0+b) over the sliced
+// dims times their strides in `in`.  Entries with s0+b >= s_end are zero.
+cudaError_t launch_slice_gather(int precision, const void* in, void* out, const GenericDesc& d,
+                                int nsl, const int64_t* sl_dim, const int64_t* sl_stride,
+                                int64_t s0, int64_t nb, int64_t s_end, cudaStream_t stream);
+// Neumaier FP64 sum over the batch axis: acc[e] += sum_b X[e + n*b].
+cudaError_t launch_slice_sum(int precision, const void* X, int64_t n, int64_t nb,
+                             double* acc, double* comp, cudaStream_t stream);
+// Split-precision tensor-core GEMM-class contraction (pq_tc.cu).  Returns
+// cudaErrorNotSupported when the shape is not eligible.
+cudaError_t launch_tc(int precision, const void* A, const void* B, void* C, const GemmDesc& d,
+                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
+size_t tc_scratch_bytes(int precision, const GemmDesc& d);
+bool tc_eligible(int precision, const GemmDesc& d);
+
+}  // namespace pq
+
+struct pq_ctx {
+  pq::Ctx impl;
+};

@@ -1,0 +1,746 @@
+// Plan executor: compile a whole pairwise contraction of a network once, then
+// execute it many times (directly, from a captured CUDA graph, or sliced in
+// batches with an FP64 compensated sum over slices).
+//
+// Follows the plan-execution semantics of src/layer2.jl:294-321
+// (contract_network! with a pair plan) and the slicing of
+// src/layer2/slicing.jl:37-110, with the GB300-specific changes:
+//   * all intermediate buffers live in one arena whose offsets come from a
+//     liveness analysis at compile time (no allocation while executing);
+//   * the final permutation to the requested output order is folded into the
+//     last contraction's index map;
+//   * slices are not materialised as separate networks: sliced leaves are
+//     gathered for a batch of slices at once (the batch becomes a shared mode
+//     of every intermediate that depends on a sliced leaf) and sub-trees that
+//     touch no sliced leaf are computed once per run.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <set>
+
+#include "pq_internal.h"
+
+namespace pq {
+int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, Tensor& t);
+int check_status(Ctx* ctx);
+}  // namespace pq
+
+using namespace pq;
+
+namespace {
+
+struct Step {
+  int x = -1, y = -1;  // SSA operands
+  PairPlan pp;
+  size_t off = 0;      // arena offset of the result
+  size_t bytes = 0;
+  bool batched = false;
+  bool is_copy = false;  // single-leaf network: result = permuted copy of x
+};
+
+struct Compiled {
+  int nleaves = 0;
+  std::vector<std::vector<int>> labels;    // per SSA value
+  std::vector<std::vector<int64_t>> dims;  // per SSA value
+  std::vector<Step> steps;                 // in execution order
+  std::vector<int> order;                  // steps' original indices
+  size_t arena_bytes = 0;
+  size_t scratch_bytes = 0;
+  int result_ssa = -1;
+  double cmacs = 0;
+  int64_t max_elems = 0;
+  int64_t launches = 0;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Liveness-driven first-fit arena assignment.  `pinned[v]` values are never
+// released once computed (used for sliced execution).
+void assign_arena(Compiled& cp, size_t elem, const std::vector<char>& pinned) {
+  const int nv = (int)cp.labels.size();
+  std::vector<int> last_use(nv, -1);
+  for (int i = 0; i < (int)cp.steps.size(); ++i) {
+    last_use[cp.steps[i].x] = i;
+    if (cp.steps[i].y >= 0) last_use[cp.steps[i].y] = i;
+  }
+  std::map<size_t, size_t> free_blocks;  // offset -> size
+  size_t top = 0;
+  auto take = [&](size_t sz) -> size_t {
+    for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+      if (it->second >= sz) {
+        size_t off = it->first, rem = it->second - sz;
+        free_blocks.erase(it);
+        if (rem) free_blocks[off + sz] = rem;
+        return off;
+      }
+    }
+    size_t off = top;
+    top += sz;
+    return off;
+  };
+  auto give = [&](size_t off, size_t sz) {
+    auto it = free_blocks.emplace(off, sz).first;
+    auto nx = std::next(it);
+    if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_blocks.erase(nx);
+    }
+    if (it != free_blocks.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_blocks.erase(it);
+      }
+    }
+  };
+  std::vector<size_t> voff(nv, 0), vsz(nv, 0);
+  for (int i = 0; i < (int)cp.steps.size(); ++i) {
+    Step& s = cp.steps[i];
+    int r = cp.nleaves + cp.order[i];
+    size_t sz = align_up(std::max<size_t>(s.bytes, 16), 256);
+    s.off = take(sz);
+    voff[r] = s.off;
+    vsz[r] = sz;
+    for (int v : {s.x, s.y}) {
+      if (v < cp.nleaves || v < 0) continue;
+      if (last_use[v] == i && !pinned[v] && v != cp.result_ssa) give(voff[v], vsz[v]);
+    }
+  }
+  cp.arena_bytes = top;
+}
+
+}  // namespace
+
+struct pq_plan {
+  Ctx* ctx = nullptr;
+  int nleaves = 0;
+  int nlabels = 0;
+  std::vector<std::vector<int>> leaf_labels;
+  std::vector<std::vector<int64_t>> leaf_dims;
+  std::vector<int64_t> label_dims;
+  std::vector<int> steps_in;  // 2*n_steps SSA operands as given
+  std::vector<int> out_labels;
+  Compiled cp;
+  void* arena = nullptr;
+  size_t arena_cap = 0;
+  void* scratch = nullptr;
+  size_t scratch_cap = 0;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<const void*> graph_ptrs;
+  // sliced execution state
+  std::vector<int> sl_labels;
+  int sl_batch = 0;
+  Compiled scp;
+  std::vector<int> sl_leaf_of;             // SSA leaf -> index into sl_leafbuf (or -1)
+  std::vector<size_t> sl_leaf_off;         // offsets of gathered leaves in arena (after scp arena)
+  std::vector<GenericDesc> sl_leaf_desc;
+  std::vector<std::vector<int64_t>> sl_leaf_sdim, sl_leaf_sstride;
+  size_t sl_total_bytes = 0;
+  double* d_acc = nullptr;  // 2*n complex sum + 2*n compensation
+  int64_t out_elems = 0;
+};
+
+namespace {
+
+// Compile `steps` (SSA pairs in execution order) for the given leaf labels.
+bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& leaf_labels,
+             const std::vector<int64_t>& label_dims, const std::vector<int>& steps,
+             const std::vector<int>& out_labels, const std::vector<int>& exec_order,
+             const std::vector<char>* batched_leaf, Compiled& cp, std::string& err) {
+  cp = Compiled();
+  const int nl = (int)leaf_labels.size();
+  const int ns = (int)steps.size() / 2;
+  cp.nleaves = nl;
+  cp.labels.assign(nl + std::max(ns, 1), {});
+  cp.dims.assign(nl + std::max(ns, 1), {});
+  for (int i = 0; i < nl; ++i) {
+    cp.labels[i] = leaf_labels[i];
+    for (int l : leaf_labels[i]) {
+      if (l < 0 || l >= (int)label_dims.size()) {
+        err = "leaf label out of range";
+        return false;
+      }
+      cp.dims[i].push_back(label_dims[l]);
+    }
+  }
+  for (int l : out_labels)
+    if (l < 0 || l >= (int)label_dims.size()) {
+      err = "output label out of range";
+      return false;
+    }
+  // label multiplicities among live values (+ output)
+  std::vector<int> cnt(label_dims.size(), 0);
+  for (int i = 0; i < nl; ++i)
+    for (int l : leaf_labels[i]) cnt[l]++;
+  std::set<int> outset(out_labels.begin(), out_labels.end());
+  for (int l : out_labels) cnt[l]++;
+  std::vector<char> live(nl + ns, 0), defined(nl + ns, 0), batched(nl + ns, 0);
+  for (int i = 0; i < nl; ++i) {
+    live[i] = defined[i] = 1;
+    if (batched_leaf) batched[i] = (*batched_leaf)[i];
+  }
+  if (ns == 0) {
+    if (nl != 1) {
+      err = "a plan without steps needs exactly one leaf";
+      return false;
+    }
+    // single leaf: result is the leaf permuted into output order
+    Step s;
+    s.x = 0;
+    s.is_copy = true;
+    std::vector<int> la = leaf_labels[0];
+    std::set<int> ls(la.begin(), la.end());
+    if (ls != outset || out_labels.size() != la.size()) {
+      err = "output labels do not match the single leaf";
+      return false;
+    }
+    if (!analyse_pair(la, cp.dims[0], {}, {}, out_labels, precision, s.pp, err)) return false;
+    s.bytes = (size_t)s.pp.csize * elem;
+    cp.steps.push_back(s);
+    cp.order.push_back(0);
+    cp.labels[nl] = out_labels;
+    cp.dims[nl] = s.pp.c_dims;
+    cp.result_ssa = nl;
+    cp.max_elems = s.pp.csize;
+    cp.launches = 1;
+    std::vector<char> pinned(nl + 1, 0);
+    assign_arena(cp, elem, pinned);
+    return true;
+  }
+  // first pass in given order to define labels (must be a valid SSA program)
+  std::vector<Step> tmp(ns);
+  for (int i = 0; i < ns; ++i) {
+    int x = steps[2 * i], y = steps[2 * i + 1];
+    if (x < 0 || y < 0 || x >= nl + i || y >= nl + i || x == y) {
+      err = "step " + std::to_string(i) + " has an invalid operand";
+      return false;
+    }
+    if (!live[x] || !live[y]) {
+      err = "step " + std::to_string(i) + " uses a consumed operand";
+      return false;
+    }
+    live[x] = live[y] = 0;
+    for (int l : cp.labels[x]) cnt[l]--;
+    for (int l : cp.labels[y]) cnt[l]--;
+    const bool last = (i == ns - 1);
+    std::vector<int> lr;
+    if (last) {
+      lr = out_labels;
+    } else {
+      for (int l : cp.labels[x])
+        if (cnt[l] > 0) lr.push_back(l);
+      for (int l : cp.labels[y])
+        if (cnt[l] > 0 && std::find(lr.begin(), lr.end(), l) == lr.end()) lr.push_back(l);
+    }
+    if (last) {
+      // everything not in the output must be summed now
+      std::set<int> have(cp.labels[x].begin(), cp.labels[x].end());
+      have.insert(cp.labels[y].begin(), cp.labels[y].end());
+      for (int l : out_labels)
+        if (!have.count(l)) {
+          err = "output label " + std::to_string(l) + " does not reach the last step";
+          return false;
+        }
+    }
+    int r = nl + i;
+    Step& s = tmp[i];
+    s.x = x;
+    s.y = y;
+    s.batched = batched[x] || batched[y];
+    batched[r] = s.batched;
+    if (!analyse_pair(cp.labels[x], cp.dims[x], cp.labels[y], cp.dims[y], lr, precision, s.pp, err)) {
+      err = "step " + std::to_string(i) + ": " + err;
+      return false;
+    }
+    s.bytes = (size_t)s.pp.csize * elem;
+    cp.labels[r] = lr;
+    cp.dims[r] = s.pp.c_dims;
+    for (int l : lr) cnt[l]++;
+    live[r] = 1;
+  }
+  int nlive = 0;
+  for (int v = 0; v < nl + ns; ++v) nlive += live[v];
+  if (nlive != 1 || !live[nl + ns - 1]) {
+    err = "plan does not contract the network to a single tensor (" + std::to_string(nlive) + " left)";
+    return false;
+  }
+  cp.result_ssa = nl + ns - 1;
+  for (int i = 0; i < ns; ++i) {
+    int idx = exec_order.empty() ? i : exec_order[i];
+    cp.steps.push_back(tmp[idx]);
+    cp.order.push_back(idx);
+    const PairPlan& p = tmp[idx].pp;
+    cp.cmacs += (double)p.csize * (double)p.ksize;
+    cp.max_elems = std::max(cp.max_elems, p.csize);
+    cp.launches += (p.kclass == KC_TC) ? 4 : 1;
+  }
+  size_t sb = 0;
+  for (auto& s : cp.steps)
+    if (s.pp.kclass == KC_TC) sb = std::max(sb, tc_scratch_bytes(precision, s.pp.m));
+  cp.scratch_bytes = sb;
+  std::vector<char> pinned(nl + ns, 0);
+  if (batched_leaf) {
+    // values computed once (not batched) but read by batched steps stay put
+    for (auto& s : cp.steps)
+      if (s.batched)
+        for (int v : {s.x, s.y})
+          if (v >= nl && !batched[v]) pinned[v] = 1;
+  }
+  assign_arena(cp, elem, pinned);
+  return true;
+}
+
+cudaError_t run_step(pq_plan* p, const Step& s, const void* A, const void* B, void* C) {
+  Ctx* ctx = p->ctx;
+  ctx->launches += (s.pp.kclass == KC_TC) ? 4 : 1;
+  if (s.is_copy) return launch_permute(ctx->precision, A, 0, C, s.pp.g, ctx->stream);
+  switch (s.pp.kclass) {
+    case KC_TC:
+      return launch_tc(ctx->precision, A, B, C, s.pp.m, p->scratch, p->scratch_cap, ctx->stream);
+    case KC_GEMM:
+      return launch_gemm(ctx->precision, A, B, C, s.pp.m, ctx->stream);
+    default:
+      return launch_generic(ctx->precision, A, B, C, s.pp.g, ctx->stream);
+  }
+}
+
+// Pointers of every SSA value for one execution.
+void resolve(pq_plan* p, const Compiled& cp, const std::vector<const void*>& leaf_ptrs,
+             std::vector<const void*>& vptr) {
+  vptr.assign(cp.labels.size(), nullptr);
+  for (int i = 0; i < cp.nleaves; ++i) vptr[i] = leaf_ptrs[i];
+  for (size_t i = 0; i < cp.steps.size(); ++i)
+    vptr[cp.nleaves + cp.order[i]] = (const char*)p->arena + cp.steps[i].off;
+}
+
+int ensure_buffers(pq_plan* p, size_t arena, size_t scratch) {
+  Ctx* ctx = p->ctx;
+  if (arena > p->arena_cap) {
+    if (p->arena) dev_free(ctx, p->arena, p->arena_cap);
+    p->arena = nullptr;
+    p->arena_cap = 0;
+    int st = dev_alloc(ctx, arena, &p->arena);
+    if (st) return st;
+    p->arena_cap = arena;
+    if (p->gexec) {
+      cudaGraphExecDestroy(p->gexec);
+      p->gexec = nullptr;
+    }
+  }
+  if (scratch > p->scratch_cap) {
+    if (p->scratch) dev_free(ctx, p->scratch, p->scratch_cap);
+    p->scratch = nullptr;
+    p->scratch_cap = 0;
+    int st = dev_alloc(ctx, scratch, &p->scratch);
+    if (st) return st;
+    p->scratch_cap = scratch;
+  }
+  return PQ_OK;
+}
+
+int leaf_pointers(pq_plan* p, const int64_t* leaf_ids, std::vector<const void*>& ptrs) {
+  Ctx* ctx = p->ctx;
+  ptrs.resize(p->nleaves);
+  for (int i = 0; i < p->nleaves; ++i) {
+    auto it = ctx->tensors.find(leaf_ids[i]);
+    if (it == ctx->tensors.end())
+      return fail(ctx, PQ_ERR_NOT_FOUND, "plan: no tensor " + std::to_string(leaf_ids[i]) + " for leaf " +
+                                             std::to_string(i));
+    const Tensor& t = it->second;
+    // a leaf may be stored with any shape whose size matches (e.g. a reshaped
+    // gate); its labels' extents define the interpretation
+    int64_t want = 1;
+    for (auto d : p->leaf_dims[i]) want *= d;
+    if (t.size != want)
+      return fail(ctx, PQ_ERR_INVALID, "plan: tensor " + std::to_string(leaf_ids[i]) + " has " +
+                                           std::to_string(t.size) + " elements, leaf " + std::to_string(i) +
+                                           " needs " + std::to_string(want));
+    ptrs[i] = t.ptr;
+  }
+  return PQ_OK;
+}
+
+int launch_all(pq_plan* p, const Compiled& cp, const std::vector<const void*>& leaf_ptrs, bool only_batched,
+               bool only_unbatched) {
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> vptr;
+  resolve(p, cp, leaf_ptrs, vptr);
+  for (size_t i = 0; i < cp.steps.size(); ++i) {
+    const Step& s = cp.steps[i];
+    if (only_batched && !s.batched) continue;
+    if (only_unbatched && s.batched) continue;
+    const void* A = vptr[s.x];
+    const void* B = s.y >= 0 ? vptr[s.y] : nullptr;
+    void* C = (char*)p->arena + s.off;
+    cudaError_t e = run_step(p, s, A, B, C);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "plan step launch");
+  }
+  return PQ_OK;
+}
+
+size_t result_off(const Compiled& cp) {
+  for (size_t i = 0; i < cp.steps.size(); ++i)
+    if (cp.nleaves + cp.order[i] == cp.result_ssa || (cp.steps[i].is_copy)) return cp.steps[i].off;
+  return 0;
+}
+
+int store_result(pq_plan* p, int64_t out_id) {
+  Ctx* ctx = p->ctx;
+  const auto& dims = p->cp.dims[p->cp.result_ssa];
+  Tensor t;
+  int st = alloc_tensor(ctx, dims, t);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(t.ptr, (const char*)p->arena + result_off(p->cp), t.bytes,
+                                  cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) {
+    dev_free(ctx, t.ptr, t.bytes);
+    return cuda_fail(ctx, e, "plan result copy");
+  }
+  auto it = ctx->tensors.find(out_id);
+  if (it != ctx->tensors.end()) {
+    dev_free(ctx, it->second.ptr, it->second.bytes);
+    it->second = std::move(t);
+  } else {
+    ctx->tensors.emplace(out_id, std::move(t));
+  }
+  return PQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_plan_create(pq_ctx* c, int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                   const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
+                   const int32_t* out_labels, pq_plan** out) {
+  if (!c || !out) return PQ_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  *out = nullptr;
+  if (n_leaves < 1 || n_labels < 0 || n_steps < 0 || n_out < 0 || !leaf_ranks || (n_labels && !label_dims) ||
+      (n_steps && !steps) || (n_out && !out_labels))
+    return fail(ctx, PQ_ERR_INVALID, "plan_create: bad arguments");
+  if (n_steps != n_leaves - 1) return fail(ctx, PQ_ERR_INVALID, "plan_create: a plan needs n_leaves-1 steps");
+  pq_plan* p = new pq_plan();
+  p->ctx = ctx;
+  p->nleaves = n_leaves;
+  p->nlabels = n_labels;
+  p->label_dims.assign(label_dims, label_dims + n_labels);
+  for (auto d : p->label_dims)
+    if (d < 1) {
+      delete p;
+      return fail(ctx, PQ_ERR_INVALID, "plan_create: label extents must be >= 1");
+    }
+  int pos = 0;
+  for (int i = 0; i < n_leaves; ++i) {
+    if (leaf_ranks[i] < 0 || leaf_ranks[i] > PQ_MAX_RANK) {
+      delete p;
+      return fail(ctx, PQ_ERR_INVALID, "plan_create: bad leaf rank");
+    }
+    std::vector<int> l(leaf_labels + pos, leaf_labels + pos + leaf_ranks[i]);
+    pos += leaf_ranks[i];
+    std::vector<int64_t> d;
+    for (int x : l) d.push_back((x >= 0 && x < n_labels) ? p->label_dims[x] : 0);
+    p->leaf_labels.push_back(l);
+    p->leaf_dims.push_back(d);
+  }
+  p->steps_in.assign(steps, steps + 2 * n_steps);
+  p->out_labels.assign(out_labels, out_labels + n_out);
+  std::string err;
+  if (!compile(ctx->precision, ctx->elem, p->leaf_labels, p->label_dims, p->steps_in, p->out_labels, {}, nullptr,
+               p->cp, err)) {
+    delete p;
+    return fail(ctx, PQ_ERR_INVALID, "plan_create: " + err);
+  }
+  *out = p;
+  return PQ_OK;
+}
+
+int pq_plan_destroy(pq_plan* p) {
+  if (!p) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->arena) dev_free(ctx, p->arena, p->arena_cap);
+  if (p->scratch) dev_free(ctx, p->scratch, p->scratch_cap);
+  if (p->d_acc) dev_free(ctx, p->d_acc, (size_t)p->out_elems * 32);
+  delete p;
+  return PQ_OK;
+}
+
+int pq_plan_info(pq_plan* p, double* cmacs, int64_t* max_elems, int64_t* arena_bytes, int64_t* launches) {
+  if (!p) return PQ_ERR_INVALID;
+  if (cmacs) *cmacs = p->cp.cmacs;
+  if (max_elems) *max_elems = p->cp.max_elems;
+  if (arena_bytes) *arena_bytes = (int64_t)p->cp.arena_bytes;
+  if (launches) *launches = p->cp.launches;
+  return PQ_OK;
+}
+
+int pq_plan_execute(pq_plan* p, const int64_t* leaf_ids, int64_t out_id) {
+  if (!p || !leaf_ids) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> ptrs;
+  int st = leaf_pointers(p, leaf_ids, ptrs);
+  if (st) return st;
+  st = ensure_buffers(p, p->cp.arena_bytes, p->cp.scratch_bytes);
+  if (st) return st;
+  bool replay = p->gexec && p->graph_ptrs.size() == ptrs.size();
+  if (replay)
+    for (size_t i = 0; i < ptrs.size(); ++i)
+      if (p->graph_ptrs[i] != ptrs[i]) replay = false;
+  if (replay) {
+    cudaError_t e = cudaGraphLaunch(p->gexec, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
+    ctx->launches += p->cp.launches;
+  } else {
+    st = launch_all(p, p->cp, ptrs, false, false);
+    if (st) return st;
+  }
+  return store_result(p, out_id);
+}
+
+int pq_plan_capture(pq_plan* p, const int64_t* leaf_ids, int64_t out_id) {
+  if (!p || !leaf_ids) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> ptrs;
+  int st = leaf_pointers(p, leaf_ids, ptrs);
+  if (st) return st;
+  st = ensure_buffers(p, p->cp.arena_bytes, p->cp.scratch_bytes);
+  if (st) return st;
+  if (p->gexec) {
+    cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "capture sync");
+  e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "begin capture");
+  int64_t before = ctx->launches;
+  st = launch_all(p, p->cp, ptrs, false, false);
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->launches = before;
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "end capture");
+  e = cudaGraphInstantiate(&p->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    p->gexec = nullptr;
+    return cuda_fail(ctx, e, "graph instantiate");
+  }
+  p->graph_ptrs.assign(ptrs.begin(), ptrs.end());
+  return pq_plan_execute(p, leaf_ids, out_id);
+}
+
+int pq_plan_profile(pq_plan* p, const int64_t* leaf_ids, int64_t out_id, float* ms) {
+  if (!p || !leaf_ids || !ms) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> ptrs;
+  int st = leaf_pointers(p, leaf_ids, ptrs);
+  if (st) return st;
+  st = ensure_buffers(p, p->cp.arena_bytes, p->cp.scratch_bytes);
+  if (st) return st;
+  std::vector<const void*> vptr;
+  resolve(p, p->cp, ptrs, vptr);
+  const size_t n = p->cp.steps.size();
+  std::vector<cudaEvent_t> ev(n + 1);
+  for (auto& x : ev) cudaEventCreate(&x);
+  cudaEventRecord(ev[0], ctx->stream);
+  cudaError_t e = cudaSuccess;
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+    const Step& s = p->cp.steps[i];
+    e = run_step(p, s, vptr[s.x], s.y >= 0 ? vptr[s.y] : nullptr, (char*)p->arena + s.off);
+    cudaEventRecord(ev[i + 1], ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
+  for (size_t i = 0; i < n; ++i) {
+    float t = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+    ms[p->cp.order[i]] = t;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "plan profile");
+  return store_result(p, out_id);
+}
+
+int pq_plan_step_features(pq_plan* p, double* feats) {
+  if (!p || !feats) return PQ_ERR_INVALID;
+  const double elem = (double)p->ctx->elem;
+  for (size_t i = 0; i < p->cp.steps.size(); ++i) {
+    const PairPlan& q = p->cp.steps[i].pp;
+    double* f = feats + 8 * p->cp.order[i];
+    f[0] = std::log2((double)q.asize);
+    f[1] = std::log2((double)q.bsize);
+    f[2] = std::log2((double)q.csize);
+    f[3] = std::log2((double)q.ksize);
+    f[4] = std::log2((double)q.run_a);
+    f[5] = std::log2((double)q.run_b);
+    f[6] = (double)q.kclass;
+    f[7] = elem * (double)(q.asize + q.bsize + q.csize);
+  }
+  return PQ_OK;
+}
+
+int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int32_t* sliced_labels,
+                       int64_t slice_begin, int64_t slice_end, int batch, int reset_sum) {
+  if (!p || !leaf_ids || n_sliced < 0 || (n_sliced && !sliced_labels) || batch < 1) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  if (n_sliced > kMaxModes) return fail(ctx, PQ_ERR_UNSUPPORTED, "run_sliced: too many sliced labels");
+  std::vector<int> S(sliced_labels, sliced_labels + n_sliced);
+  int64_t total = 1;
+  for (int l : S) {
+    if (l < 0 || l >= p->nlabels) return fail(ctx, PQ_ERR_INVALID, "run_sliced: sliced label out of range");
+    if (std::find(p->out_labels.begin(), p->out_labels.end(), l) != p->out_labels.end())
+      return fail(ctx, PQ_ERR_INVALID, "run_sliced: an output label cannot be sliced");
+    total *= p->label_dims[l];
+  }
+  if (slice_begin < 0 || slice_end > total || slice_begin > slice_end)
+    return fail(ctx, PQ_ERR_INVALID, "run_sliced: slice range outside [0, " + std::to_string(total) + ")");
+  std::vector<const void*> ptrs;
+  int st = leaf_pointers(p, leaf_ids, ptrs);
+  if (st) return st;
+  // (re)compile the batched network when the slicing or batch changes
+  if (S != p->sl_labels || batch != p->sl_batch || p->scp.steps.empty()) {
+    const int beta = p->nlabels;  // the batch label
+    std::vector<int64_t> ldims = p->label_dims;
+    ldims.push_back(batch);
+    std::vector<std::vector<int>> ll(p->nleaves);
+    std::vector<char> bl(p->nleaves, 0);
+    p->sl_leaf_of.assign(p->nleaves, -1);
+    p->sl_leaf_off.clear();
+    p->sl_leaf_desc.clear();
+    p->sl_leaf_sdim.clear();
+    p->sl_leaf_sstride.clear();
+    for (int i = 0; i < p->nleaves; ++i) {
+      const auto& lab = p->leaf_labels[i];
+      bool hit = false;
+      for (int l : lab)
+        if (std::find(S.begin(), S.end(), l) != S.end()) hit = true;
+      if (!hit) {
+        ll[i] = lab;
+        continue;
+      }
+      bl[i] = 1;
+      std::vector<int64_t> strides(lab.size());
+      int64_t acc = 1;
+      for (size_t j = 0; j < lab.size(); ++j) {
+        strides[j] = acc;
+        acc *= p->leaf_dims[i][j];
+      }
+      GenericDesc g;
+      std::memset(&g, 0, sizeof(g));
+      int64_t ksz = 1;
+      for (size_t j = 0; j < lab.size(); ++j) {
+        if (std::find(S.begin(), S.end(), lab[j]) != S.end()) continue;
+        ll[i].push_back(lab[j]);
+        g.cdim[g.nc] = p->leaf_dims[i][j];
+        g.csa[g.nc] = strides[j];
+        g.clog[g.nc] = -1;
+        g.nc++;
+        ksz *= p->leaf_dims[i][j];
+      }
+      g.csize = ksz;
+      g.ksize = 1;
+      ll[i].push_back(beta);
+      std::vector<int64_t> sd, ss;
+      for (int l : S) {
+        sd.push_back(p->label_dims[l]);
+        auto it = std::find(lab.begin(), lab.end(), l);
+        ss.push_back(it == lab.end() ? 0 : strides[it - lab.begin()]);
+      }
+      p->sl_leaf_of[i] = (int)p->sl_leaf_desc.size();
+      p->sl_leaf_desc.push_back(g);
+      p->sl_leaf_sdim.push_back(sd);
+      p->sl_leaf_sstride.push_back(ss);
+    }
+    std::vector<int> outl = p->out_labels;
+    outl.push_back(beta);
+    // execution order: steps that touch no sliced leaf first
+    const int ns = (int)p->steps_in.size() / 2;
+    std::vector<char> b(p->nleaves + ns, 0);
+    for (int i = 0; i < p->nleaves; ++i) b[i] = bl[i];
+    std::vector<int> first, second;
+    for (int i = 0; i < ns; ++i) {
+      b[p->nleaves + i] = b[p->steps_in[2 * i]] || b[p->steps_in[2 * i + 1]];
+      (b[p->nleaves + i] ? second : first).push_back(i);
+    }
+    std::vector<int> order = first;
+    order.insert(order.end(), second.begin(), second.end());
+    std::string err;
+    if (!compile(ctx->precision, ctx->elem, ll, ldims, p->steps_in, outl, order, &bl, p->scp, err))
+      return fail(ctx, PQ_ERR_INVALID, "run_sliced: " + err);
+    // gathered leaf buffers after the arena
+    size_t off = align_up(p->scp.arena_bytes, 256);
+    for (size_t j = 0; j < p->sl_leaf_desc.size(); ++j) {
+      p->sl_leaf_off.push_back(off);
+      off += align_up((size_t)p->sl_leaf_desc[j].csize * batch * ctx->elem, 256);
+    }
+    p->sl_total_bytes = off;
+    p->sl_labels = S;
+    p->sl_batch = batch;
+  }
+  // output accumulators
+  int64_t oe = 1;
+  for (auto d : p->scp.dims[p->scp.result_ssa]) oe *= d;
+  oe /= batch;
+  if (oe != p->out_elems || !p->d_acc) {
+    if (p->d_acc) dev_free(ctx, p->d_acc, (size_t)p->out_elems * 32);
+    p->d_acc = nullptr;
+    p->out_elems = oe;
+    st = dev_alloc(ctx, (size_t)oe * 32, (void**)&p->d_acc);
+    if (st) return st;
+    reset_sum = 1;
+  }
+  if (reset_sum) {
+    cudaError_t e = cudaMemsetAsync(p->d_acc, 0, (size_t)oe * 32, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "run_sliced reset");
+  }
+  st = ensure_buffers(p, std::max(p->sl_total_bytes, p->cp.arena_bytes), p->scp.scratch_bytes);
+  if (st) return st;
+  // leaf pointers for the batched network
+  std::vector<const void*> lp(p->nleaves);
+  for (int i = 0; i < p->nleaves; ++i)
+    lp[i] = p->sl_leaf_of[i] >= 0 ? (const void*)((char*)p->arena + p->sl_leaf_off[p->sl_leaf_of[i]]) : ptrs[i];
+  // unbatched part once
+  st = launch_all(p, p->scp, lp, false, true);
+  if (st) return st;
+  const size_t res_off = result_off(p->scp);
+  for (int64_t s0 = slice_begin; s0 < slice_end; s0 += batch) {
+    int64_t nb = std::min<int64_t>(batch, slice_end - s0);
+    for (int i = 0; i < p->nleaves; ++i) {
+      int j = p->sl_leaf_of[i];
+      if (j < 0) continue;
+      cudaError_t e = launch_slice_gather(ctx->precision, ptrs[i], (char*)p->arena + p->sl_leaf_off[j],
+                                          p->sl_leaf_desc[j], (int)S.size(), p->sl_leaf_sdim[j].data(),
+                                          p->sl_leaf_sstride[j].data(), s0, batch, s0 + nb, ctx->stream);
+      ctx->launches++;
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "slice gather");
+    }
+    st = launch_all(p, p->scp, lp, true, false);
+    if (st) return st;
+    cudaError_t e = launch_slice_sum(ctx->precision, (const char*)p->arena + res_off, oe, nb, p->d_acc,
+                                     p->d_acc + 2 * oe, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "slice sum");
+  }
+  return PQ_OK;
+}
+
+int pq_sliced_result(pq_plan* p, double* out, int64_t n) {
+  if (!p || !out) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  if (!p->d_acc || n < p->out_elems) return fail(ctx, PQ_ERR_INVALID, "sliced_result: no result or buffer too small");
+  std::vector<double> h((size_t)p->out_elems * 4);
+  cudaError_t e = cudaMemcpyAsync(h.data(), p->d_acc, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sliced_result copy");
+  int st = check_status(ctx);
+  if (st) return st;
+  for (int64_t i = 0; i < 2 * p->out_elems; ++i) out[i] = h[i] + h[2 * p->out_elems + i];
+  return PQ_OK;
+}
+
+}  // extern "C"

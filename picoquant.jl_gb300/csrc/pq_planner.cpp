@@ -1,0 +1,368 @@
+// Host planners: Boltzmann-greedy pair selection (the flop-count planner) and
+// the choice of labels to slice.
+//
+// The pair heuristic is the Gray & Kourtis cost used by the reference's
+// bgreedy (src/layer2/bgreedy_contraction.jl:76-94):
+//     energy(A, B) = |C| - alpha * (|A| + |B|)
+// sampled with weight exp(-(energy - min_energy) / (tau * max(1, |min_energy|)))
+// (the temperature is relative to the scale of the energies so the sampler
+// stays meaningful when tensor sizes span many orders of magnitude).  Only
+// pairs that share a label are candidates (pairs without a shared label are
+// outer products; they are taken last, smallest first, as
+// src/layer2.jl:260-264 does for disjoint pieces).  The plan with the fewest
+// complex multiply-adds (src/backends.jl:30-41) over `n_trials` draws wins.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <random>
+#include <set>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/pqgb300.h"
+
+namespace {
+
+struct Net {
+  std::vector<std::vector<int>> labels;  // per SSA value
+  std::vector<double> l2size;            // log2 of the element count
+};
+
+struct Trial {
+  std::vector<int32_t> steps;
+  double cmacs = 0;
+  double max_l2 = 0;
+};
+
+double l2size_of(const std::vector<int>& l, const std::vector<double>& l2dim) {
+  double s = 0;
+  for (int x : l) s += l2dim[x];
+  return s;
+}
+
+Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, const std::vector<double>& l2dim,
+                  const std::vector<int>& out_labels, double alpha, double tau, std::mt19937_64& rng) {
+  const int nl = n_leaves;
+  const int nv = 2 * nl - 1;
+  const int nlab = (int)l2dim.size();
+  std::vector<std::vector<int>> lab(nv);
+  std::vector<double> l2(nv, 0);
+  std::vector<char> live(nv, 0);
+  std::vector<int> cnt(nlab, 0);
+  std::vector<std::vector<int>> holders(nlab);  // live values per label (lazy)
+  for (int i = 0; i < nl; ++i) {
+    lab[i] = leaves[i];
+    l2[i] = l2size_of(lab[i], l2dim);
+    live[i] = 1;
+    for (int x : lab[i]) {
+      cnt[x]++;
+      holders[x].push_back(i);
+    }
+  }
+  for (int x : out_labels) cnt[x]++;
+  Trial t;
+  // candidate scores, keyed by (a, b) with a < b
+  std::map<std::pair<int, int>, double> cand;
+  auto result_labels = [&](int a, int b, std::vector<int>& r, double& l2c, double& l2all) {
+    r.clear();
+    l2all = 0;
+    for (int x : lab[a]) {
+      l2all += l2dim[x];
+      int c = cnt[x] - 1;
+      if (std::find(lab[b].begin(), lab[b].end(), x) != lab[b].end()) c--;
+      if (c > 0) r.push_back(x);
+    }
+    for (int x : lab[b]) {
+      if (std::find(lab[a].begin(), lab[a].end(), x) != lab[a].end()) continue;
+      l2all += l2dim[x];
+      if (cnt[x] - 1 > 0) r.push_back(x);
+    }
+    l2c = l2size_of(r, l2dim);
+  };
+  std::vector<int> tmp;
+  auto score = [&](int a, int b) {
+    double l2c, l2all;
+    result_labels(a, b, tmp, l2c, l2all);
+    return std::exp2(l2c) - alpha * (std::exp2(l2[a]) + std::exp2(l2[b]));
+  };
+  auto add_pairs_of = [&](int v) {
+    std::set<int> nb;
+    for (int x : lab[v])
+      for (int u : holders[x])
+        if (u != v && live[u]) nb.insert(u);
+    for (int u : nb) {
+      auto key = std::make_pair(std::min(u, v), std::max(u, v));
+      cand[key] = score(key.first, key.second);
+    }
+  };
+  for (int i = 0; i < nl; ++i) add_pairs_of(i);
+  int next = nl;
+  int nlive = nl;
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  std::vector<std::pair<int, int>> keys;
+  std::vector<double> w;
+  while (nlive > 1) {
+    int a = -1, b = -1;
+    if (!cand.empty()) {
+      double emin = INFINITY;
+      for (auto& kv : cand) emin = std::min(emin, kv.second);
+      if (tau <= 0) {
+        // deterministic greedy with random tie-break
+        keys.clear();
+        for (auto& kv : cand)
+          if (kv.second <= emin) keys.push_back(kv.first);
+        auto k = keys[std::uniform_int_distribution<size_t>(0, keys.size() - 1)(rng)];
+        a = k.first;
+        b = k.second;
+      } else {
+        const double T = tau * std::max(1.0, std::fabs(emin));
+        keys.clear();
+        w.clear();
+        double tot = 0;
+        for (auto& kv : cand) {
+          double x = std::exp(-(kv.second - emin) / T);
+          keys.push_back(kv.first);
+          w.push_back(x);
+          tot += x;
+        }
+        double r = U(rng) * tot;
+        size_t k = 0;
+        for (; k + 1 < w.size(); ++k) {
+          r -= w[k];
+          if (r <= 0) break;
+        }
+        a = keys[k].first;
+        b = keys[k].second;
+      }
+    } else {
+      // disjoint pieces: outer product of the two smallest
+      int s1 = -1, s2 = -1;
+      for (int v = 0; v < next; ++v) {
+        if (!live[v]) continue;
+        if (s1 < 0 || l2[v] < l2[s1]) {
+          s2 = s1;
+          s1 = v;
+        } else if (s2 < 0 || l2[v] < l2[s2]) {
+          s2 = v;
+        }
+      }
+      a = std::min(s1, s2);
+      b = std::max(s1, s2);
+    }
+    double l2c, l2all;
+    std::vector<int> r;
+    result_labels(a, b, r, l2c, l2all);
+    t.cmacs += std::exp2(l2all);
+    t.max_l2 = std::max(t.max_l2, l2c);
+    t.steps.push_back(a);
+    t.steps.push_back(b);
+    // retire a, b
+    live[a] = live[b] = 0;
+    for (int x : lab[a]) cnt[x]--;
+    for (int x : lab[b]) cnt[x]--;
+    for (auto it = cand.begin(); it != cand.end();) {
+      if (it->first.first == a || it->first.second == a || it->first.first == b || it->first.second == b)
+        it = cand.erase(it);
+      else
+        ++it;
+    }
+    int v = next++;
+    lab[v] = r;
+    l2[v] = l2c;
+    live[v] = 1;
+    for (int x : r) {
+      cnt[x]++;
+      auto& h = holders[x];
+      h.erase(std::remove_if(h.begin(), h.end(), [&](int u) { return !live[u]; }), h.end());
+      h.push_back(v);
+    }
+    nlive--;
+    // scores of pairs sharing a label whose count changed are stale; refresh
+    // every candidate touching a neighbour of v, then add v's pairs
+    std::set<int> touched;
+    for (int x : r)
+      for (int u : holders[x])
+        if (u != v && live[u]) touched.insert(u);
+    for (auto& kv : cand)
+      if (touched.count(kv.first.first) || touched.count(kv.first.second))
+        kv.second = score(kv.first.first, kv.first.second);
+    add_pairs_of(v);
+  }
+  return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_plan_greedy(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                   const int64_t* label_dims, int n_out, const int32_t* out_labels, double alpha, double tau,
+                   int n_trials, uint64_t seed, int32_t* steps, double* cmacs, int64_t* max_elems) {
+  if (n_leaves < 1 || !leaf_ranks || (n_labels && !label_dims) || (n_out && !out_labels) || n_trials < 1 ||
+      (n_leaves > 1 && !steps))
+    return PQ_ERR_INVALID;
+  std::vector<double> l2dim(n_labels);
+  for (int i = 0; i < n_labels; ++i) {
+    if (label_dims[i] < 1) return PQ_ERR_INVALID;
+    l2dim[i] = std::log2((double)label_dims[i]);
+  }
+  std::vector<std::vector<int>> leaves(n_leaves);
+  int pos = 0;
+  for (int i = 0; i < n_leaves; ++i) {
+    if (leaf_ranks[i] < 0) return PQ_ERR_INVALID;
+    for (int j = 0; j < leaf_ranks[i]; ++j) {
+      int x = leaf_labels[pos++];
+      if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+      leaves[i].push_back(x);
+    }
+  }
+  std::vector<int> outl(out_labels, out_labels + n_out);
+  for (int x : outl)
+    if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+  std::mt19937_64 rng(seed);
+  Trial best;
+  best.cmacs = INFINITY;
+  for (int t = 0; t < n_trials; ++t) {
+    // the first draw is the plain greedy order (tau = 0)
+    Trial tr = greedy_once(n_leaves, leaves, l2dim, outl, alpha, t == 0 ? 0.0 : tau, rng);
+    if (tr.cmacs < best.cmacs || (tr.cmacs == best.cmacs && tr.max_l2 < best.max_l2)) best = tr;
+  }
+  if (n_leaves > 1) std::memcpy(steps, best.steps.data(), best.steps.size() * sizeof(int32_t));
+  if (cmacs) *cmacs = n_leaves > 1 ? best.cmacs : 0.0;
+  if (max_elems) *max_elems = (int64_t)std::llround(std::exp2(best.max_l2));
+  return PQ_OK;
+}
+
+int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                          const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
+                          const int32_t* out_labels, int max_sliced, double log2_target, int32_t* sliced,
+                          int* n_sliced) {
+  if (n_leaves < 1 || !leaf_ranks || n_steps != n_leaves - 1 || (n_steps && !steps) || !sliced || !n_sliced ||
+      max_sliced < 0)
+    return PQ_ERR_INVALID;
+  std::vector<double> l2dim(n_labels);
+  for (int i = 0; i < n_labels; ++i) {
+    if (label_dims[i] < 1) return PQ_ERR_INVALID;
+    l2dim[i] = std::log2((double)label_dims[i]);
+  }
+  const int nv = n_leaves + n_steps;
+  std::vector<std::vector<int>> lab(nv);
+  std::vector<std::vector<int>> all(nv);      // labels involved in the step producing v
+  std::vector<std::vector<char>> dep(nv);     // labels of leaves in v's subtree
+  int pos = 0;
+  std::vector<int> cnt(n_labels, 0);
+  for (int i = 0; i < n_leaves; ++i) {
+    for (int j = 0; j < leaf_ranks[i]; ++j) {
+      int x = leaf_labels[pos++];
+      if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+      lab[i].push_back(x);
+      cnt[x]++;
+    }
+    dep[i].assign(n_labels, 0);
+    for (int x : lab[i]) dep[i][x] = 1;
+  }
+  std::vector<char> is_out(n_labels, 0);
+  for (int i = 0; i < n_out; ++i) {
+    is_out[out_labels[i]] = 1;
+    cnt[out_labels[i]]++;
+  }
+  for (int s = 0; s < n_steps; ++s) {
+    int a = steps[2 * s], b = steps[2 * s + 1];
+    if (a < 0 || b < 0 || a >= n_leaves + s || b >= n_leaves + s) return PQ_ERR_INVALID;
+    int v = n_leaves + s;
+    for (int x : lab[a]) cnt[x]--;
+    for (int x : lab[b]) cnt[x]--;
+    std::vector<int> r, u;
+    for (int x : lab[a]) {
+      u.push_back(x);
+      if (cnt[x] > 0) r.push_back(x);
+    }
+    for (int x : lab[b]) {
+      if (std::find(lab[a].begin(), lab[a].end(), x) != lab[a].end()) continue;
+      u.push_back(x);
+      if (cnt[x] > 0) r.push_back(x);
+    }
+    for (int x : r) cnt[x]++;
+    lab[v] = r;
+    all[v] = u;
+    dep[v].assign(n_labels, 0);
+    for (int x = 0; x < n_labels; ++x) dep[v][x] = dep[a][x] | dep[b][x];
+  }
+  // Current (sliced) log2 size of every value, log2 cost of every step, and
+  // whether the step varies with the slice (depends on a sliced leaf).
+  std::vector<char> chosen(n_labels, 0);
+  std::vector<int> S;
+  std::vector<double> sz(nv, 0), cc(nv, 0);
+  std::vector<char> varies(nv, 0);
+  for (int v = 0; v < nv; ++v) {
+    for (int x : lab[v]) sz[v] += l2dim[x];
+    for (int x : all[v]) cc[v] += l2dim[x];
+  }
+  double nsl = 0;
+  auto cur_max = [&]() {
+    double m = 0;
+    for (int v = 0; v < nv; ++v) m = std::max(m, sz[v]);
+    return m;
+  };
+  double cmax = cur_max();
+  while ((int)S.size() < max_sliced && cmax > log2_target + 1e-9) {
+    // only labels carried by a largest value can lower the maximum
+    std::vector<char> cand(n_labels, 0);
+    for (int v = 0; v < nv; ++v)
+      if (sz[v] >= cmax - 1e-9)
+        for (int x : lab[v])
+          if (!chosen[x] && !is_out[x]) cand[x] = 1;
+    int best = -1;
+    // objective, lexicographic: largest intermediate, how many values have
+    // that size, total cost of all slices
+    auto count_at = [&](double m) {
+      int c = 0;
+      for (int v = 0; v < nv; ++v)
+        if (sz[v] >= m - 1e-9) ++c;
+      return c;
+    };
+    double bmax = cmax, bcost = INFINITY;
+    int bcnt = count_at(cmax);
+    const int cur_cnt = bcnt;
+    for (int x = 0; x < n_labels; ++x) {
+      if (!cand[x]) continue;
+      double m = 0, cost = 0;
+      std::vector<double> nsz(nv);
+      for (int v = 0; v < nv; ++v) {
+        bool has = std::find(lab[v].begin(), lab[v].end(), x) != lab[v].end();
+        nsz[v] = sz[v] - (has ? l2dim[x] : 0);
+        m = std::max(m, nsz[v]);
+        if (v < n_leaves) continue;
+        bool inv = std::find(all[v].begin(), all[v].end(), x) != all[v].end();
+        bool var = varies[v] || dep[v][x];
+        cost += std::exp2(cc[v] - (inv ? l2dim[x] : 0) + (var ? nsl + l2dim[x] : 0));
+      }
+      int cntm = 0;
+      for (int v = 0; v < nv; ++v)
+        if (nsz[v] >= m - 1e-9) ++cntm;
+      bool better = m < bmax - 1e-9 || (std::fabs(m - bmax) <= 1e-9 && (cntm < bcnt || (cntm == bcnt && cost < bcost)));
+      if (better) {
+        best = x;
+        bmax = m;
+        bcnt = cntm;
+        bcost = cost;
+      }
+    }
+    if (best < 0 || (bmax >= cmax - 1e-9 && bcnt >= cur_cnt)) break;
+    chosen[best] = 1;
+    S.push_back(best);
+    nsl += l2dim[best];
+    for (int v = 0; v < nv; ++v) {
+      if (std::find(lab[v].begin(), lab[v].end(), best) != lab[v].end()) sz[v] -= l2dim[best];
+      if (std::find(all[v].begin(), all[v].end(), best) != all[v].end()) cc[v] -= l2dim[best];
+      if (dep[v][best]) varies[v] = 1;
+    }
+    cmax = cur_max();
+  }
+  for (size_t i = 0; i < S.size(); ++i) sliced[i] = S[i];
+  *n_sliced = (int)S.size();
+  return PQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+"""Host-side logic on CPU: the C ABI loads and exports every declared symbol,
+the native planners produce valid plans, and the product's graph layer (run
+over a numpy test backend) reproduces the oracle's bookkeeping."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "pqgb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|void)\s+(pq_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(pq):
+    from pqgb300 import _lib as L
+
+    lib = L.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 30
+    for s in syms:
+        assert hasattr(lib, s), f"libpqgb300.so does not export {s}"
+    bound = {name for name, _, _ in L.SIGNATURES}
+    assert set(syms) <= bound | L.OPTIONAL, set(syms) - bound
+
+
+def test_null_handles_are_rejected(pq):
+    from pqgb300 import _lib as L
+
+    lib = L.lib()
+    assert lib.pq_ctx_destroy(None) == L.PQ_ERR_INVALID
+    assert lib.pq_plan_destroy(None) == L.PQ_ERR_INVALID
+    assert lib.pq_ctx_sync(None) == L.PQ_ERR_INVALID
+    assert lib.pq_last_error(None) == b"null context"
+
+
+def _ssa_valid(steps, n):
+    live = set(range(n))
+    for i in range(len(steps) // 2):
+        a, b = steps[2 * i], steps[2 * i + 1]
+        assert a in live and b in live and a != b
+        live -= {a, b}
+        live.add(n + i)
+    assert live == {2 * n - 2}
+
+
+def _leaves(pq, net):
+    return pq.planning._leaf_arrays(net, pq.open_output_edges(net))
+
+
+@pytest.mark.parametrize("rows,cols,depth", [(2, 2, 3), (2, 3, 5), (3, 3, 6)])
+def test_greedy_plan_valid_and_cost_consistent(pq, O, host_backend, rows, cols, depth):
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=3)
+    net = pq.build_network(n, gates, backend=host_backend)
+    pq.add_input(net, "0" * n)
+    nodes, ranks, flat, dims, label_of = _leaves(pq, net)
+    outl = [label_of[e] for e in pq.open_output_edges(net)]
+    steps, cm, mx = pq.greedy_steps(ranks, flat, dims, outl, 1.0, 1.0, 6, 1)
+    _ssa_valid(steps, len(ranks))
+    c2, m2 = pq.planning.plan_cost(ranks, flat, dims, steps, outl)
+    assert abs(cm - c2) <= 1e-9 * c2 and m2 == mx
+    # executing the plan with the oracle backend gives the state vector
+    plan = pq.steps_to_pairs(net, steps, nodes)
+    pq.contract_network(net, plan)
+    out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
+    assert np.max(np.abs(out - O.statevector(n, gates))) < 1e-12
+
+
+def test_sweep_plan_single_amplitude(pq, O, host_backend):
+    gates = pq.random_grid_gates(3, 3, 6, seed=5)
+    bits = "101100110"
+    net = pq.build_network(9, gates, backend=host_backend, decompose=True)
+    pq.add_input(net, "0" * 9)
+    pq.add_output(net, bits)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    _ssa_valid(steps, len(net.nodes))
+    pq.contract_network(net, pq.steps_to_pairs(net, steps))
+    amp = pq.load_tensor_data(net, "result")
+    ref = O.statevector(9, gates)[O.amplitude_index(bits)]
+    assert abs(complex(np.asarray(amp).reshape(-1)[0]) - ref) < 1e-13
+
+
+def test_slice_chooser_reduces_size(pq, host_backend):
+    gates = pq.random_grid_gates(4, 4, 8, seed=9)
+    net = pq.build_network(16, gates, backend=host_backend, decompose=True)
+    pq.add_input(net, "0" * 16)
+    pq.add_output(net, "0" * 16)
+    nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
+    steps, cm, mx, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    lib_steps = pq.planning
+    from pqgb300 import _lib as L
+    import ctypes as C
+
+    out = (C.c_int32 * 8)()
+    ns = C.c_int()
+    rc = L.lib().pq_plan_choose_slices(len(ranks), L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
+                                       L.arr(C.c_int64, dims), len(steps) // 2, L.arr(C.c_int32, steps), 0,
+                                       L.arr(C.c_int32, []), 4, 0.0, out, C.byref(ns))
+    assert rc == 0 and ns.value >= 1
+    chosen = set(out[: ns.value])
+    # recompute the largest intermediate with those labels fixed
+    sliced_dims = [1 if i in chosen else d for i, d in enumerate(dims)]
+    _, mx2 = lib_steps.plan_cost(ranks, flat, sliced_dims, steps, [])
+    assert mx2 < mx
+
+
+def test_product_graph_matches_oracle_metrics(pq, host_backend):
+    # the reference's 8/44/124 golden through the product's L2 code
+    net = pq.build_network(3, [(pq.H, [1]), (pq.CX, [1, 2]), (pq.CX, [1, 2]), (pq.CX, [1, 3])],
+                           backend=host_backend)
+    pq.add_input(net, "000")
+    pq.full_wavefunction_contraction(net, "vector")
+    m = host_backend.metrics
+    assert (m.max_tensor_size, m.total_space_allocated, m.flops) == (8, 44, 124)
+
+
+def test_product_generators_match_oracle(pq, O):
+    a = pq.random_grid_gates(3, 4, 5, seed=17)
+    b = O.random_grid_gates(3, 4, 5, 17)
+    assert len(a) == len(b)
+    for (ua, qa), (ub, qb) in zip(a, b):
+        assert qa == qb and np.array_equal(ua, ub)
+    for (ua, qa), (ub, qb) in zip(pq.qft_gates(6), O.qft_gates(6)):
+        assert qa == qb and np.allclose(ua, ub, atol=0, rtol=0)
+    for U, _ in pq.random_grid_gates(2, 2, 3, seed=1):
+        if U.shape == (2, 2):
+            assert np.allclose(U @ U.conj().T, np.eye(2), atol=1e-14)
+            assert abs(np.linalg.det(U) - 1) < 1e-14
+
+
+def test_product_slicing_host_logic(pq, O, host_backend):
+    n = 4
+    circ = O.simple_preparation_gates(n, 2, np.random.default_rng(2)) + O.qft_gates(n)
+    full = O.statevector(n, circ)
+    tot = 0
+    for p in range(1, 5):
+        be = type(host_backend)()
+        net = pq.build_network(n, circ, decompose=True, backend=be)
+        pq.add_input(net, "0" * n)
+        bl, bv = pq.partition_network_on_virtual_bonds(net, 4, p)
+        pq.slice_tensor_network(net, bl, bv)
+        pq.full_wavefunction_contraction(net, "vector")
+        tot = tot + pq.load_tensor_data(net, "result")
+    assert np.max(np.abs(tot - full)) < 1e-13
+
+
+def test_wavefunction_steps_match_reference_order(pq, O, host_backend):
+    gates = pq.random_grid_gates(2, 3, 4, seed=2)
+    net = pq.build_network(6, gates, backend=host_backend)
+    pq.add_input(net, "0" * 6)
+    steps = pq.wavefunction_steps(net)
+    _ssa_valid(steps, len(net.nodes))
+    pq.contract_network(net, pq.steps_to_pairs(net, steps))
+    out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
+    assert np.max(np.abs(out - O.statevector(6, gates))) < 1e-13
