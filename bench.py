@@ -1,0 +1,515 @@
+"""Benchmark: amplitudes/s of tensor-network contraction on one GB300.
+
+Default workload (the configuration the headline metric is quoted on): one
+single amplitude of a 6x6-qubit random grid circuit of depth 16 (Haar SU(2)
+layers + CZ on four alternating edge patterns, CZ split into bond-2 virtual
+edges), contracted along the qubit-sweep flop-count plan with 10 bond-2 edges
+sliced -> 1024 identical-shape slices, batched per launch and summed on the
+device in FP64 (Neumaier).  A step = all 1024 slices of one amplitude.
+
+Also: --workload grid4x5_d12_amps (1024 amplitudes of a 4x5 depth-12 circuit).
+
+Rank 0 prints one JSON line.  `--impl reference` times the FP64 CPU
+restatement (numpy tensordot -> BLAS zgemm, all host cores) on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "amplitudes/s on 1 GB300: mixed-prec+learned plan vs plain FP64 @ rel err≤1e-6"
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+
+
+def load_peaks():
+    try:
+        return json.loads(PEAKS_FILE.read_text()), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026, rank=0, target=28.0):
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=seed)
+    bits = pq.random_bitstrings(n, 1, seed=seed + 1 + rank)[0]
+    be = pq.GB300Backend(precision)
+    net = pq.build_network(n, gates, decompose=True, backend=be)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    t0 = time.perf_counter()
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    sliced = plan.choose_slices(max_sliced=n_sliced, log2_target=target)
+    t_plan = time.perf_counter() - t0
+    return dict(be=be, net=net, plan=plan, sliced=sliced, gates=gates, bits=bits, cmacs=cm, max_elems=mx,
+                planner=name, t_plan=t_plan, n=n)
+
+
+def leaf_host_data(pq, w, dtype):
+    """Host copies of every leaf (what a caller uploads each end-to-end step)."""
+    be, plan, net = w["be"], w["plan"], w["net"]
+    out = []
+    for nl in plan.leaves:
+        lab = net.nodes[nl].data_label
+        out.append((lab, np.asfortranarray(be.load_tensor_data(lab)).astype(dtype)))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="grid6x6_d16_sliced", choices=["grid6x6_d16_sliced", "grid4x5_d12_amps"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "3xbf16", "c128"])
+    ap.add_argument("--batch", type=int, default=0, help="slices per launch (0: sized from memory)")
+    ap.add_argument("--cpu-log2", type=float, default=31.0, help="log2 complex MACs of the CPU sample")
+    ap.add_argument("--slice-target", type=float, default=28.0,
+                    help="log2 elements allowed per slice intermediate when choosing sliced bonds")
+    ap.add_argument("--fp64", default="full", choices=["full", "skip"],
+                    help="also run the plain complex-FP64 GPU path on the same amplitude")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return run_reference(args)
+    return run_gb300(args, world, rank)
+
+
+def run_reference(args):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import tn_oracle as O  # the FP64 CPU restatement (reference arm)
+
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    cores = os.cpu_count()
+    rows, cols, depth = (6, 6, 16) if args.workload == "grid6x6_d16_sliced" else (4, 5, 12)
+    val, sample = cpu_sample(pq, O, args, rows, cols, depth)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "amplitudes/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": workload_config(args, rows, cols, depth),
+            "cpu_baseline": {"value": val, "unit": "amplitudes/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "amplitudes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(args, rows, cols, depth):
+    if args.workload == "grid6x6_d16_sliced":
+        return {"workload": f"grid{rows}x{cols}_depth{depth}_sliced_single_amplitude", "qubits": rows * cols,
+                "depth": depth, "sliced_bonds": 10, "slices": 1024, "batch": args.batch,
+                "plan": "qubit-sweep (flop-count planner)", "l2": "flushed between steps (256 MiB write)"}
+    return {"workload": f"grid{rows}x{cols}_depth{depth}_1024_amplitudes", "qubits": rows * cols, "depth": depth,
+            "amplitudes_per_step": 1024, "plan": "flop-count planner (open outputs + gather)",
+            "l2": "flushed between steps (256 MiB write)"}
+
+
+def _cpu_sample_sliced(pq, O, args, rows=6, cols=6, depth=16):
+    """CPU FP64 rate on the plan's heaviest pairwise step, shrunk to about
+    2^(args.cpu_log2) complex multiply-adds by fixing free modes of the larger
+    operand; the amplitude time is the plan's total complex multiply-adds over
+    that measured rate."""
+    host = _HostStore()
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
+    bits = pq.random_bitstrings(n, 1, seed=2027)[0]
+    net = pq.build_network(n, gates, decompose=True, backend=host)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
+    # find the heaviest step and its operand labels
+    labs, pos = [], 0
+    for r in ranks:
+        labs.append(list(flat[pos:pos + r]))
+        pos += r
+    cnt = {}
+    for l in labs:
+        for x in l:
+            cnt[x] = cnt.get(x, 0) + 1
+    best = None
+    for i in range(len(steps) // 2):
+        la, lb = labs[steps[2 * i]], labs[steps[2 * i + 1]]
+        for x in la + lb:
+            cnt[x] -= 1
+        union = list(dict.fromkeys(la + lb))
+        keep = [x for x in union if cnt[x] > 0]
+        for x in keep:
+            cnt[x] += 1
+        labs.append(keep)
+        c = float(np.prod([dims[x] for x in union], dtype=np.float64))
+        if best is None or c > best[0]:
+            best = (c, la, lb)
+    c, la, lb = best
+    common = [x for x in la if x in lb]
+    # shrink: fix free modes of the larger operand until ~2^cpu_log2 MACs
+    big, small = (la, lb) if np.prod([dims[x] for x in la]) >= np.prod([dims[x] for x in lb]) else (lb, la)
+    fixed = set()
+    work = c
+    for x in big:
+        if work <= 2.0 ** args.cpu_log2:
+            break
+        if x not in common:
+            fixed.add(x)
+            work /= dims[x]
+    rng = np.random.default_rng(0)
+    shp_b = [1 if x in fixed else dims[x] for x in big]
+    shp_s = [dims[x] for x in small]
+    A = rng.standard_normal(shp_b) + 1j * rng.standard_normal(shp_b)
+    B = rng.standard_normal(shp_s) + 1j * rng.standard_normal(shp_s)
+    axes = ([big.index(x) for x in common], [small.index(x) for x in common])
+    np.tensordot(A, B, axes=axes)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        np.tensordot(A, B, axes=axes)
+        reps += 1
+        if time.perf_counter() - t0 > 2.0:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    rate = work / dt  # complex MACs / s
+    desc = (f"heaviest step of the plan ({np.log2(c):.1f} log2 complex MACs) shrunk to 2^{np.log2(work):.1f} "
+            f"by fixing free modes, numpy tensordot FP64 (BLAS zgemm, {os.cpu_count()} threads) at "
+            f"{rate * 8 / 1e9:.1f} GFLOP/s; amplitude time = plan total 2^{np.log2(cm):.2f} complex MACs / rate")
+    return rate / cm, desc
+
+
+def _choose(pq, ranks, flat, dims, steps, k):
+    import ctypes as C
+
+    from pqgb300 import _lib as L
+
+    out = (C.c_int32 * k)()
+    ns = C.c_int()
+    rc = L.lib().pq_plan_choose_slices(len(ranks), L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
+                                       L.arr(C.c_int64, dims), len(steps) // 2, L.arr(C.c_int32, steps), 0,
+                                       L.arr(C.c_int32, []), k, 0.0, out, C.byref(ns))
+    L.check(rc, None, "choose_slices")
+    return [out[i] for i in range(ns.value)]
+
+
+class _HostStore:
+    """Minimal host tensor store for building the CPU-baseline network."""
+
+    def __init__(self):
+        from pqgb300.backend import Metrics
+
+        self.tensors = {}
+        self.metrics = Metrics()
+
+    def save_tensor_data(self, label, data):
+        self.tensors[label] = np.asarray(data, dtype=np.complex128)
+
+    def shape(self, label):
+        return self.tensors[label].shape
+
+
+def _cpu_sample_amps(pq, O, n_amps, rows=4, cols=5, depth=12):
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=2024)
+    t0 = time.perf_counter()
+    sv = O.statevector(n, gates)
+    bits = pq.random_bitstrings(n, 1024, seed=7)
+    _ = sv[[O.amplitude_index(b) for b in bits]]
+    dt = time.perf_counter() - t0
+    return 1024 / dt, "full 1024 amplitudes via FP64 numpy state vector (tensordot per gate)"
+
+
+def cpu_sample(pq, O, args, rows, cols, depth):
+    """Time the FP64 CPU restatement on a bounded sample; returns (amplitudes/s, description)."""
+    if args.workload == "grid6x6_d16_sliced":
+        return _cpu_sample_sliced(pq, O, args, rows, cols, depth)
+    return _cpu_sample_amps(pq, O, 1024, rows, cols, depth)
+
+
+def run_gb300(args, world, rank):
+    import torch
+
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    peaks, peaks_kind = load_peaks()
+    prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}
+    prec_name = args.precision if args.precision != "auto" else "c64"
+    precision = prec_map[prec_name]
+
+    if args.workload == "grid6x6_d16_sliced":
+        rows, cols, depth = 6, 6, 16
+        w = build_sliced(pq, precision, rows, cols, depth, rank=rank, target=args.slice_target)
+        be, plan, sliced = w["be"], w["plan"], w["sliced"]
+        if args.batch <= 0:
+            args.batch = plan.auto_batch(sliced)
+
+        def step():
+            return plan.run_sliced(sliced, batch=args.batch)
+
+        amps_per_step = 1
+    else:
+        rows, cols, depth = 4, 5, 12
+        n = rows * cols
+        gates = pq.random_grid_gates(rows, cols, depth, seed=2024)
+        be = pq.GB300Backend(precision)
+        net = pq.build_network(n, gates, backend=be)
+        pq.add_input(net, "0" * n)
+        steps_, cm, mx, name = pq.planning.best_flop_plan(net, trials=4)
+        plan = pq.NetworkPlan(net, steps=steps_)
+        plan.capture()
+        bits = pq.random_bitstrings(n, 1024, seed=7)
+        w = dict(be=be, net=net, plan=plan, cmacs=cm, max_elems=mx, planner=name, bits=bits)
+
+        def step():
+            return plan.amplitudes(bits)
+
+        amps_per_step = 1024
+
+    import ctypes as C
+
+    sp = C.c_void_p()
+    be.lib.pq_ctx_stream(be.ctx, C.byref(sp))
+    ext = torch.cuda.ExternalStream(sp.value)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    be.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    launches0 = be.launch_count()
+    times = []
+    result = None
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        result = step()
+        e1.record(ext)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    launches = be.launch_count() - launches0
+    clk = clocks.stop()
+    t_total = sum(times) / 1e3
+    if dist:
+        t = torch.tensor([t_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+        dist.barrier()
+    value = world * amps_per_step * args.steps / t_total
+
+    # ---- end to end: host leaf upload + contraction + result download -----
+    e2e = None
+    if args.workload == "grid6x6_d16_sliced":
+        host = leaf_host_data(pq, w, np.complex128 if precision == pq.PREC_C128 else np.complex64)
+        h2d = sum(a.nbytes for _, a in host)
+
+        def e2e_step():
+            for lab, a in host:
+                be.save_tensor_data(lab, a)
+            return plan.run_sliced(sliced, batch=args.batch)
+
+        e2e_step()
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            e2e_step()
+            ts.append(time.perf_counter() - t0)
+        e2e = {"value": world / (sum(ts) / len(ts)), "unit": "amplitudes/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": 16}
+    else:
+        def e2e_step():
+            return plan.amplitudes(w["bits"])
+
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            e2e_step()
+            ts.append(time.perf_counter() - t0)
+        e2e = {"value": world * 1024 / (sum(ts) / len(ts)), "unit": "amplitudes/s",
+               "h2d_bytes_per_step": 1024 * 8, "d2h_bytes_per_step": 1024 * 16}
+
+    line = None
+    if rank == 0:
+        line = report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, launches, clk, e2e, peaks,
+                      peaks_kind, prec_name, precision, result, world)
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, launches, clk, e2e, peaks, peaks_kind,
+           prec_name, precision, result, world):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import tn_oracle as O  # the FP64 CPU restatement, for the cpu_baseline leg only
+
+    extra = {}
+    roof = None
+    if args.workload == "grid6x6_d16_sliced":
+        sliced = w["sliced"]
+        ms, batched, feats = plan.profile_sliced(sliced, batch=args.batch)
+        roof, kinfo = roofline_from_profile(ms, batched, feats, peaks, peaks_kind, 2 ** len(sliced) // args.batch)
+        extra["kernel_classes"] = kinfo
+        # the plain complex-FP64 CUDA path on the same amplitude, and the error
+        # of this precision against it
+        if args.fp64 == "full":
+            w64 = build_sliced(pq, pq.PREC_C128, rows, cols, depth, target=args.slice_target)
+            b64 = w64["plan"].auto_batch(w64["sliced"])
+            t0 = time.perf_counter()
+            a64 = w64["plan"].run_sliced(w64["sliced"], batch=b64)
+            t64 = time.perf_counter() - t0
+            extra["plain_fp64_gpu"] = {"value": 1.0 / t64, "unit": "amplitudes/s",
+                                       "sample": "the same amplitude, all slices, complex128 FP64 kernels"}
+            extra["speedup_vs_plain_fp64"] = value / extra["plain_fp64_gpu"]["value"]
+            extra["rel_err_vs_fp64"] = abs(result - a64) / abs(a64)
+            w64["plan"].close()
+            w64["be"].close()
+        extra["amplitude"] = [float(np.real(result)), float(np.imag(result))]
+        w64["plan"].close()
+        w64["be"].close()
+        extra["plan"] = {"planner": w["planner"], "cmacs_unsliced": w["cmacs"], "max_elems_unsliced": w["max_elems"],
+                         "sliced_bonds": len(sliced), "planning_s": w["t_plan"]}
+    else:
+        extra["plan"] = {"planner": w["planner"], "cmacs": w["cmacs"], "max_elems": w["max_elems"]}
+        ms = w["plan"].profile()
+        feats = w["plan"].features()
+        roof, kinfo = roofline_from_profile(ms, np.zeros(len(ms), bool), feats, peaks, peaks_kind, 1)
+        extra["kernel_classes"] = kinfo
+    cpu_val, cpu_sample_desc = cpu_sample(__import__("__graft_entry__").load_package(), O, args, rows, cols, depth)
+    line = {
+        "metric": METRIC, "value": value, "unit": "amplitudes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"c64": "c64", "3xtf32": "c64(3xtf32)",
+                                                           "3xbf16": "c64(3xbf16)", "c128": "c128"}[prec_name],
+        "data": "synthetic (seeded random circuits)", "config": workload_config(args, rows, cols, depth),
+        "precision": prec_name, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
+        "cpu_baseline": {"value": cpu_val, "unit": "amplitudes/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": cpu_sample_desc},
+    }
+    line.update(extra)
+    return line
+
+
+def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks):
+    """Dominant kernel class by device time; achieved algorithmic FLOP/s or
+    bytes/s of that class over its measured launch time."""
+    names = {0: "generic", 1: "gemm_simt", 2: "tcgen05", 3: "copy"}
+    info = {}
+    for t, b, f in zip(ms, batched, feats):
+        k = int(f[6])
+        d = info.setdefault(names.get(k, str(k)), {"ms_per_run": 0.0, "launches_per_run": 0, "flops": 0.0,
+                                                    "bytes": 0.0, "ms_profiled": 0.0})
+        rep = nchunks if b else 1
+        d["ms_per_run"] += t * rep
+        d["launches_per_run"] += rep
+        d["flops"] += 8.0 * 2 ** f[2] * 2 ** f[3] * rep
+        d["bytes"] += f[7] * rep
+    tot = sum(d["ms_per_run"] for d in info.values()) or 1.0
+    for d in info.values():
+        d["share"] = d["ms_per_run"] / tot
+    dom = max(info, key=lambda k: info[k]["ms_per_run"])
+    d = info[dom]
+    secs = d["ms_per_run"] / 1e3
+    if dom in ("gemm_simt", "tcgen05"):
+        ach = d["flops"] / secs / 1e12
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": None, "kernel": dom, "peak_source": f"{peaks_kind} bf16 sustained",
+                "per_launch_ms": d["ms_per_run"] / d["launches_per_run"]}
+    else:
+        ach = d["bytes"] / secs / 1e9
+        peak = peaks.get("hbm_gbs")
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                "kernel": dom, "peak_source": f"{peaks_kind} hbm copy",
+                "per_launch_ms": d["ms_per_run"] / d["launches_per_run"]}
+    return roof, info
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -183,6 +183,14 @@ int pq_plan_run_sliced(pq_plan* plan, const int64_t* leaf_ids, int n_sliced,
                        int batch, int reset_sum);
 /* Copy the FP64 slice sum (interleaved re/im, n elements) to host memory. */
 int pq_sliced_result(pq_plan* plan, double* out, int64_t n);
+/* Profile sliced execution: runs the once-per-run steps and one batch of
+ * `batch` slices with CUDA events around every step.  For each step i
+ * (original plan order) writes ms[i], batched[i] (1 if the step runs once per
+ * batch of slices, 0 if once per run) and 8 shape features feats[8*i..]
+ * (as pq_plan_step_features, for the batched network). */
+int pq_plan_profile_sliced(pq_plan* plan, const int64_t* leaf_ids, int n_sliced,
+                           const int32_t* sliced_labels, int batch, float* ms,
+                           int32_t* batched, double* feats);
 
 /* ---- planning ---------------------------------------------------------------
  * Boltzmann-greedy flop-count planner, after src/layer2/bgreedy_contraction.jl:17-66:

@@ -745,6 +745,57 @@ def statevector(n, gates, init=None):
     return psi
 
 
+def execute_ssa_plan(leaves, leaf_labels, steps, out_labels=()):
+    """Execute SSA pair steps over numpy leaves with integer labels (the CPU
+    equivalent of a compiled plan).  A label is summed once no other live
+    tensor and no output carries it; the result's modes follow ``out_labels``.
+    Each pair is one ``tensordot`` (BLAS zgemm), like TensorOperations->BLAS."""
+    vals = [np.asarray(x) for x in leaves]
+    labs = [list(l) for l in leaf_labels]
+    cnt: dict[int, int] = {}
+    for l in labs:
+        for x in l:
+            cnt[x] = cnt.get(x, 0) + 1
+    for x in out_labels:
+        cnt[x] = cnt.get(x, 0) + 1
+    for i in range(len(steps) // 2):
+        a, b = steps[2 * i], steps[2 * i + 1]
+        la, lb = labs[a], labs[b]
+        for x in la:
+            cnt[x] -= 1
+        for x in lb:
+            cnt[x] -= 1
+        common = [x for x in la if x in lb]
+        if any(cnt[x] > 0 for x in common):
+            raise ValueError("hyper-indices are not supported by the CPU plan executor")
+        C = np.tensordot(vals[a], vals[b], axes=([la.index(x) for x in common], [lb.index(x) for x in common]))
+        lc = [x for x in la if x not in common] + [x for x in lb if x not in common]
+        for x in lc:
+            cnt[x] += 1
+        vals.append(C)
+        labs.append(lc)
+        vals[a] = vals[b] = None
+    res, lr = vals[-1], labs[-1]
+    if len(out_labels):
+        res = np.transpose(res, [lr.index(x) for x in out_labels])
+    return res
+
+
+def slice_leaves(leaves, leaf_labels, sliced, dims, s):
+    """Leaves with the sliced labels fixed to the mixed-radix digits of slice
+    ``s`` (first sliced label fastest); the fixed modes are removed."""
+    vals = {}
+    for x in sliced:
+        vals[x] = s % dims[x]
+        s //= dims[x]
+    out, labs = [], []
+    for t, l in zip(leaves, leaf_labels):
+        idx = tuple(vals[x] if x in vals else slice(None) for x in l)
+        out.append(np.asarray(t)[idx])
+        labs.append([x for x in l if x not in vals])
+    return out, labs
+
+
 def amplitude_index(bitstring):
     """Index into a little-endian state vector of the output configuration
     ``bitstring`` (character i = qubit i+1)."""

@@ -85,6 +85,7 @@ SIGNATURES = [
     ("pq_plan_step_features", C.c_int, [vp, f64p]),
     ("pq_plan_run_sliced", C.c_int, [vp, i64p, C.c_int, i32p, C.c_int64, C.c_int64, C.c_int, C.c_int]),
     ("pq_sliced_result", C.c_int, [vp, f64p, C.c_int64]),
+    ("pq_plan_profile_sliced", C.c_int, [vp, i64p, C.c_int, i32p, C.c_int, f32p, i32p, f64p]),
     ("pq_plan_greedy", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_double, C.c_double,
                                  C.c_int, C.c_uint64, i32p, f64p, i64p]),
     ("pq_plan_choose_slices", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_int, i32p,

@@ -585,22 +585,25 @@ int pq_plan_step_features(pq_plan* p, double* feats) {
   return PQ_OK;
 }
 
-int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int32_t* sliced_labels,
-                       int64_t slice_begin, int64_t slice_end, int batch, int reset_sum) {
+}  // extern "C"
+
+namespace {
+
+// Validate the slicing request, (re)compile the batched network and resolve
+// the leaf pointers of the original (ptrs) and batched (lp) networks.
+int prepare_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int32_t* sliced_labels, int batch,
+                   std::vector<const void*>& ptrs, std::vector<const void*>& lp, int64_t& total) {
   if (!p || !leaf_ids || n_sliced < 0 || (n_sliced && !sliced_labels) || batch < 1) return PQ_ERR_INVALID;
   Ctx* ctx = p->ctx;
   if (n_sliced > kMaxModes) return fail(ctx, PQ_ERR_UNSUPPORTED, "run_sliced: too many sliced labels");
   std::vector<int> S(sliced_labels, sliced_labels + n_sliced);
-  int64_t total = 1;
+  total = 1;
   for (int l : S) {
     if (l < 0 || l >= p->nlabels) return fail(ctx, PQ_ERR_INVALID, "run_sliced: sliced label out of range");
     if (std::find(p->out_labels.begin(), p->out_labels.end(), l) != p->out_labels.end())
       return fail(ctx, PQ_ERR_INVALID, "run_sliced: an output label cannot be sliced");
     total *= p->label_dims[l];
   }
-  if (slice_begin < 0 || slice_end > total || slice_begin > slice_end)
-    return fail(ctx, PQ_ERR_INVALID, "run_sliced: slice range outside [0, " + std::to_string(total) + ")");
-  std::vector<const void*> ptrs;
   int st = leaf_pointers(p, leaf_ids, ptrs);
   if (st) return st;
   // (re)compile the batched network when the slicing or batch changes
@@ -683,6 +686,42 @@ int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const 
     p->sl_labels = S;
     p->sl_batch = batch;
   }
+  st = ensure_buffers(p, std::max(p->sl_total_bytes, p->cp.arena_bytes), p->scp.scratch_bytes);
+  if (st) return st;
+  lp.resize(p->nleaves);
+  for (int i = 0; i < p->nleaves; ++i)
+    lp[i] = p->sl_leaf_of[i] >= 0 ? (const void*)((char*)p->arena + p->sl_leaf_off[p->sl_leaf_of[i]]) : ptrs[i];
+  return PQ_OK;
+}
+
+cudaError_t gather_batch(pq_plan* p, const std::vector<const void*>& ptrs, int64_t s0, int64_t nb) {
+  Ctx* ctx = p->ctx;
+  for (int i = 0; i < p->nleaves; ++i) {
+    int j = p->sl_leaf_of[i];
+    if (j < 0) continue;
+    cudaError_t e = launch_slice_gather(ctx->precision, ptrs[i], (char*)p->arena + p->sl_leaf_off[j],
+                                        p->sl_leaf_desc[j], (int)p->sl_labels.size(), p->sl_leaf_sdim[j].data(),
+                                        p->sl_leaf_sstride[j].data(), s0, p->sl_batch, s0 + nb, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int32_t* sliced_labels,
+                       int64_t slice_begin, int64_t slice_end, int batch, int reset_sum) {
+  if (!p) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> ptrs, lp;
+  int64_t total = 0;
+  int st = prepare_sliced(p, leaf_ids, n_sliced, sliced_labels, batch, ptrs, lp, total);
+  if (st) return st;
+  if (slice_begin < 0 || slice_end > total || slice_begin > slice_end)
+    return fail(ctx, PQ_ERR_INVALID, "run_sliced: slice range outside [0, " + std::to_string(total) + ")");
   // output accumulators
   int64_t oe = 1;
   for (auto d : p->scp.dims[p->scp.result_ssa]) oe *= d;
@@ -699,27 +738,14 @@ int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const 
     cudaError_t e = cudaMemsetAsync(p->d_acc, 0, (size_t)oe * 32, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "run_sliced reset");
   }
-  st = ensure_buffers(p, std::max(p->sl_total_bytes, p->cp.arena_bytes), p->scp.scratch_bytes);
-  if (st) return st;
-  // leaf pointers for the batched network
-  std::vector<const void*> lp(p->nleaves);
-  for (int i = 0; i < p->nleaves; ++i)
-    lp[i] = p->sl_leaf_of[i] >= 0 ? (const void*)((char*)p->arena + p->sl_leaf_off[p->sl_leaf_of[i]]) : ptrs[i];
   // unbatched part once
   st = launch_all(p, p->scp, lp, false, true);
   if (st) return st;
   const size_t res_off = result_off(p->scp);
   for (int64_t s0 = slice_begin; s0 < slice_end; s0 += batch) {
     int64_t nb = std::min<int64_t>(batch, slice_end - s0);
-    for (int i = 0; i < p->nleaves; ++i) {
-      int j = p->sl_leaf_of[i];
-      if (j < 0) continue;
-      cudaError_t e = launch_slice_gather(ctx->precision, ptrs[i], (char*)p->arena + p->sl_leaf_off[j],
-                                          p->sl_leaf_desc[j], (int)S.size(), p->sl_leaf_sdim[j].data(),
-                                          p->sl_leaf_sstride[j].data(), s0, batch, s0 + nb, ctx->stream);
-      ctx->launches++;
-      if (e != cudaSuccess) return cuda_fail(ctx, e, "slice gather");
-    }
+    cudaError_t eg = gather_batch(p, ptrs, s0, nb);
+    if (eg != cudaSuccess) return cuda_fail(ctx, eg, "slice gather");
     st = launch_all(p, p->scp, lp, true, false);
     if (st) return st;
     cudaError_t e = launch_slice_sum(ctx->precision, (const char*)p->arena + res_off, oe, nb, p->d_acc,
@@ -727,6 +753,52 @@ int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const 
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "slice sum");
   }
+  return PQ_OK;
+}
+
+int pq_plan_profile_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int32_t* sliced_labels,
+                           int batch, float* ms, int32_t* batched, double* feats) {
+  if (!p || !ms || !batched || !feats) return PQ_ERR_INVALID;
+  Ctx* ctx = p->ctx;
+  std::vector<const void*> ptrs, lp;
+  int64_t total = 0;
+  int st = prepare_sliced(p, leaf_ids, n_sliced, sliced_labels, batch, ptrs, lp, total);
+  if (st) return st;
+  cudaError_t e = gather_batch(p, ptrs, 0, std::min<int64_t>(batch, total));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "profile gather");
+  const Compiled& cp = p->scp;
+  std::vector<const void*> vptr;
+  resolve(p, cp, lp, vptr);
+  const size_t n = cp.steps.size();
+  std::vector<cudaEvent_t> ev(n + 1);
+  for (auto& x : ev) cudaEventCreate(&x);
+  cudaEventRecord(ev[0], ctx->stream);
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+    const Step& s = cp.steps[i];
+    e = run_step(p, s, vptr[s.x], s.y >= 0 ? vptr[s.y] : nullptr, (char*)p->arena + s.off);
+    cudaEventRecord(ev[i + 1], ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
+  const double elem = (double)ctx->elem;
+  for (size_t i = 0; i < n; ++i) {
+    float t = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+    const int o = cp.order[i];
+    ms[o] = t;
+    batched[o] = cp.steps[i].batched ? 1 : 0;
+    const PairPlan& q = cp.steps[i].pp;
+    double* f = feats + 8 * o;
+    f[0] = std::log2((double)q.asize);
+    f[1] = std::log2((double)q.bsize);
+    f[2] = std::log2((double)q.csize);
+    f[3] = std::log2((double)q.ksize);
+    f[4] = std::log2((double)q.run_a);
+    f[5] = std::log2((double)q.run_b);
+    f[6] = (double)q.kclass;
+    f[7] = elem * (double)(q.asize + q.bsize + q.csize);
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "profile sliced");
   return PQ_OK;
 }
 

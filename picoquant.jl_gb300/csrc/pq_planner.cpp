@@ -289,6 +289,14 @@ int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t
     dep[v].assign(n_labels, 0);
     for (int x = 0; x < n_labels; ++x) dep[v][x] = dep[a][x] | dep[b][x];
   }
+  // Membership tables: inlab[v][x] (x is a mode of value v) and inall[v][x]
+  // (x takes part in the step producing v).
+  std::vector<std::vector<char>> inlab(nv, std::vector<char>(n_labels, 0)), inall(nv);
+  for (int v = 0; v < nv; ++v) {
+    for (int x : lab[v]) inlab[v][x] = 1;
+    inall[v].assign(n_labels, 0);
+    for (int x : all[v]) inall[v][x] = 1;
+  }
   // Current (sliced) log2 size of every value, log2 cost of every step, and
   // whether the step varies with the slice (depends on a sliced leaf).
   std::vector<char> chosen(n_labels, 0);
@@ -305,60 +313,57 @@ int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t
     for (int v = 0; v < nv; ++v) m = std::max(m, sz[v]);
     return m;
   };
-  double cmax = cur_max();
-  while ((int)S.size() < max_sliced && cmax > log2_target + 1e-9) {
-    // only labels carried by a largest value can lower the maximum
-    std::vector<char> cand(n_labels, 0);
-    for (int v = 0; v < nv; ++v)
-      if (sz[v] >= cmax - 1e-9)
-        for (int x : lab[v])
-          if (!chosen[x] && !is_out[x]) cand[x] = 1;
+  // Objective of slicing label x next: (largest intermediate clipped at the
+  // target, number of values at that size, total cost over all slices), in
+  // lexicographic order.  Once the largest intermediate is within the target
+  // only the total cost (the redundant work slicing causes) matters.
+  while ((int)S.size() < max_sliced) {
+    const double cmax = cur_max();
     int best = -1;
-    // objective, lexicographic: largest intermediate, how many values have
-    // that size, total cost of all slices
-    auto count_at = [&](double m) {
-      int c = 0;
-      for (int v = 0; v < nv; ++v)
-        if (sz[v] >= m - 1e-9) ++c;
-      return c;
-    };
-    double bmax = cmax, bcost = INFINITY;
-    int bcnt = count_at(cmax);
-    const int cur_cnt = bcnt;
+    double bkey = INFINITY, bcost = INFINITY;
+    int bcnt = 1 << 30;
     for (int x = 0; x < n_labels; ++x) {
-      if (!cand[x]) continue;
+      if (chosen[x] || is_out[x]) continue;
+      bool used = false;
+      for (int v = n_leaves; v < nv && !used; ++v) used = inall[v][x];
+      if (!used) continue;
       double m = 0, cost = 0;
-      std::vector<double> nsz(nv);
-      for (int v = 0; v < nv; ++v) {
-        bool has = std::find(lab[v].begin(), lab[v].end(), x) != lab[v].end();
-        nsz[v] = sz[v] - (has ? l2dim[x] : 0);
-        m = std::max(m, nsz[v]);
-        if (v < n_leaves) continue;
-        bool inv = std::find(all[v].begin(), all[v].end(), x) != all[v].end();
-        bool var = varies[v] || dep[v][x];
-        cost += std::exp2(cc[v] - (inv ? l2dim[x] : 0) + (var ? nsl + l2dim[x] : 0));
-      }
+      for (int v = 0; v < nv; ++v) m = std::max(m, sz[v] - (inlab[v][x] ? l2dim[x] : 0));
       int cntm = 0;
       for (int v = 0; v < nv; ++v)
-        if (nsz[v] >= m - 1e-9) ++cntm;
-      bool better = m < bmax - 1e-9 || (std::fabs(m - bmax) <= 1e-9 && (cntm < bcnt || (cntm == bcnt && cost < bcost)));
+        if (sz[v] - (inlab[v][x] ? l2dim[x] : 0) >= m - 1e-9) ++cntm;
+      for (int v = n_leaves; v < nv; ++v) {
+        const bool var = varies[v] || dep[v][x];
+        cost += std::exp2(cc[v] - (inall[v][x] ? l2dim[x] : 0) + (var ? nsl + l2dim[x] : 0));
+      }
+      const double key = std::max(m, log2_target);
+      const bool over = key > log2_target + 1e-9;
+      bool better;
+      if (key < bkey - 1e-9)
+        better = true;
+      else if (key > bkey + 1e-9)
+        better = false;
+      else if (over)
+        better = cntm < bcnt || (cntm == bcnt && cost < bcost);
+      else
+        better = cost < bcost;
       if (better) {
         best = x;
-        bmax = m;
+        bkey = key;
         bcnt = cntm;
         bcost = cost;
       }
     }
-    if (best < 0 || (bmax >= cmax - 1e-9 && bcnt >= cur_cnt)) break;
+    if (best < 0) break;
+    (void)cmax;
     chosen[best] = 1;
     S.push_back(best);
     nsl += l2dim[best];
     for (int v = 0; v < nv; ++v) {
-      if (std::find(lab[v].begin(), lab[v].end(), best) != lab[v].end()) sz[v] -= l2dim[best];
-      if (std::find(all[v].begin(), all[v].end(), best) != all[v].end()) cc[v] -= l2dim[best];
+      if (inlab[v][best]) sz[v] -= l2dim[best];
+      if (inall[v][best]) cc[v] -= l2dim[best];
       if (dep[v][best]) varies[v] = 1;
     }
-    cmax = cur_max();
   }
   for (size_t i = 0; i < S.size(); ++i) sliced[i] = S[i];
   *n_sliced = (int)S.size();

@@ -225,6 +225,62 @@ class NetworkPlan:
             return res[0]
         return res.reshape([self.dims[x] for x in self.out_labels], order="F")
 
+    def profile_sliced(self, sliced_edges, batch=64):
+        """Per-step device time (ms) of sliced execution for one batch of
+        slices, whether each step runs per batch, and per-step features."""
+        lab = [self.label_of[e] for e in sliced_edges]
+        n = len(self.steps) // 2
+        ms = (C.c_float * max(1, n))()
+        bat = (C.c_int32 * max(1, n))()
+        f = (C.c_double * max(1, 8 * n))()
+        rc = self.lib.pq_plan_profile_sliced(self.h, self.leaf_ids, len(lab), L.arr(C.c_int32, lab), int(batch),
+                                             ms, bat, f)
+        L.check(rc, self.backend.ctx, "plan_profile_sliced")
+        return (np.array(ms[:n], dtype=np.float64), np.array(bat[:n], dtype=bool),
+                np.array(f[: 8 * n], dtype=np.float64).reshape(n, 8))
+
+    def sliced_sizes(self, sliced_edges):
+        """Per step: (log2 elements of the result for one slice, whether the
+        step runs per slice)."""
+        S = {self.label_of[e] for e in sliced_edges}
+        labs, dep, pos = [], [], 0
+        for r in self.ranks:
+            l = self.flat[pos:pos + r]
+            pos += r
+            labs.append(l)
+            dep.append(bool(set(l) & S))
+        cnt: dict[int, int] = {}
+        for l in labs:
+            for x in l:
+                cnt[x] = cnt.get(x, 0) + 1
+        for x in self.out_labels:
+            cnt[x] = cnt.get(x, 0) + 1
+        out = []
+        for i in range(len(self.steps) // 2):
+            a, b = self.steps[2 * i], self.steps[2 * i + 1]
+            for x in labs[a] + labs[b]:
+                cnt[x] -= 1
+            keep = [x for x in dict.fromkeys(labs[a] + labs[b]) if cnt[x] > 0]
+            for x in keep:
+                cnt[x] += 1
+            labs.append(keep)
+            dep.append(dep[a] or dep[b])
+            out.append((sum(np.log2(self.dims[x]) for x in keep if x not in S), dep[-1]))
+        return out
+
+    def auto_batch(self, sliced_edges, budget_bytes=32 << 30, max_batch=1024):
+        """Largest power-of-two batch of slices whose per-slice intermediates
+        (three live at a time, at most) fit in ``budget_bytes``."""
+        elem = 16 if self.backend.precision == L.PREC_C128 else 8
+        big = max([s for s, b in self.sliced_sizes(sliced_edges) if b] or [0.0])
+        total = 1
+        for e in sliced_edges:
+            total *= self.dims[self.label_of[e]]
+        b = 1
+        while b * 2 <= min(max_batch, total) and 3 * elem * (2 ** big) * b * 2 <= budget_bytes:
+            b *= 2
+        return b
+
     def choose_slices(self, max_sliced=10, log2_target=0.0):
         """Labels (edge names) the slice chooser picks for this plan."""
         out = (C.c_int32 * max(1, max_sliced))()

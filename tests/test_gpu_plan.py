@@ -1,0 +1,173 @@
+"""Compiled plans (NetworkPlan): wavefunction / greedy / sweep plans, CUDA
+graph replay, many amplitudes, and sliced single amplitudes with the FP64
+compensated slice sum, all against the FP64 oracle.
+
+Tolerances: complex128 1e-12 relative, complex64 1e-6 relative (max-abs error
+over the largest reference magnitude; for single amplitudes the error is
+relative to the amplitude's magnitude scale 2^-n/2).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-12, 1: 1e-6}
+
+
+def rel(a, b):
+    a = np.asarray(a).reshape(-1)
+    b = np.asarray(b).reshape(-1)
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(params=[0, 1], ids=["c128", "c64"])
+def prec(request):
+    return request.param
+
+
+def open_net(pq, be, r, c, d, seed, decompose=False):
+    n = r * c
+    g = pq.random_grid_gates(r, c, d, seed=seed)
+    net = pq.build_network(n, g, backend=be, decompose=decompose)
+    pq.add_input(net, "0" * n)
+    return net, g
+
+
+@pytest.mark.parametrize("planner", ["wavefunction", "greedy"])
+def test_plan_state_vector(pq, O, prec, planner):
+    be = pq.GB300Backend(prec)
+    net, g = open_net(pq, be, 3, 4, 8, seed=21)
+    plan = pq.NetworkPlan(net, planner=planner, trials=4)
+    info = plan.info()
+    assert info["steps"] == len(net.nodes) - 1 and info["arena_bytes"] > 0
+    plan.execute()
+    got = plan.result().reshape(-1, order="F")
+    ref = O.statevector(12, g)
+    assert rel(got, ref) < TOL[prec]
+    # graph capture, replayed twice, gives the same result
+    plan.capture()
+    plan.execute()
+    got2 = plan.result().reshape(-1, order="F")
+    assert rel(got2, ref) < TOL[prec]
+    assert np.array_equal(got, got2)
+    # the leaves were not consumed: the interactive path still works
+    pq.full_wavefunction_contraction(net, "vector")
+    assert rel(pq.load_tensor_data(net, "result"), ref) < TOL[prec]
+    plan.close()
+    be.close()
+
+
+def test_plan_profile_and_features(pq, prec):
+    be = pq.GB300Backend(prec)
+    net, _ = open_net(pq, be, 2, 3, 4, seed=3)
+    plan = pq.NetworkPlan(net, planner="greedy", trials=2)
+    ms = plan.profile()
+    f = plan.features()
+    n = len(net.nodes) - 1
+    assert ms.shape == (n,) and np.all(ms >= 0)
+    assert f.shape == (n, 8) and np.all(np.isfinite(f))
+    plan.close()
+    be.close()
+
+
+def test_many_amplitudes_small(pq, O, prec):
+    be = pq.GB300Backend(prec)
+    net, g = open_net(pq, be, 3, 4, 8, seed=5)
+    bits = pq.random_bitstrings(12, 256, seed=1)
+    plan = pq.NetworkPlan(net, planner="wavefunction")
+    plan.capture()
+    amps = plan.amplitudes(bits)
+    sv = O.statevector(12, g)
+    ref = sv[[O.amplitude_index(b) for b in bits]]
+    assert np.max(np.abs(amps - ref)) / np.max(np.abs(sv)) < TOL[prec]
+    plan.close()
+    be.close()
+
+
+def test_config2_grid_4x5_depth12_1024_amplitudes(pq, O, prec):
+    """4x5 grid, depth 12, 1024 seeded bitstrings (config 2), c64 and c128."""
+    be = pq.GB300Backend(prec)
+    net, g = open_net(pq, be, 4, 5, 12, seed=2024)
+    bits = pq.random_bitstrings(20, 1024, seed=7)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, trials=4)
+    plan = pq.NetworkPlan(net, steps=steps)
+    plan.capture()
+    amps = plan.amplitudes(bits)
+    sv = O.statevector(20, g)
+    ref = sv[[O.amplitude_index(b) for b in bits]]
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(amps - ref)) / scale < TOL[prec]
+    plan.close()
+    be.close()
+
+
+def single_amp_net(pq, be, r, c, d, seed, bits):
+    n = r * c
+    g = pq.random_grid_gates(r, c, d, seed=seed)
+    net = pq.build_network(n, g, backend=be, decompose=True)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    return net, g
+
+
+@pytest.mark.parametrize("batch", [1, 7, 64])
+def test_sliced_single_amplitude(pq, O, prec, batch):
+    r, c, d = 3, 4, 8
+    bits = "011010011100"
+    be = pq.GB300Backend(prec)
+    net, g = single_amp_net(pq, be, r, c, d, 99, bits)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    sliced = plan.choose_slices(max_sliced=5, log2_target=0)
+    assert 1 <= len(sliced) <= 5
+    amp = plan.run_sliced(sliced, batch=batch)
+    plan.execute()
+    unsliced = complex(np.asarray(plan.result()).reshape(-1)[0])
+    ref = O.statevector(r * c, g)[O.amplitude_index(bits)]
+    scale = 2.0 ** (-(r * c) / 2)
+    assert abs(amp - ref) / scale < TOL[prec]
+    assert abs(unsliced - ref) / scale < TOL[prec]
+    # partial ranges accumulate to the same sum
+    total = 2 ** len(sliced)
+    half = total // 2
+    plan.run_sliced(sliced, batch=batch, begin=0, end=half, reset=True)
+    amp2 = plan.run_sliced(sliced, batch=batch, begin=half, end=total, reset=False)
+    assert abs(amp2 - amp) / scale < 10 * TOL[prec]
+    plan.close()
+    be.close()
+
+
+def test_config3_scaled_sliced(pq, O, prec):
+    """Config 3 in miniature: 4x4 grid, depth 10, CZ split into bond-2
+    virtual edges, 6 sliced bonds (64 identical-shape slices) summed in FP64."""
+    bits = "0110100111001010"
+    be = pq.GB300Backend(prec)
+    net, g = single_amp_net(pq, be, 4, 4, 10, 3, bits)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep", "greedy"))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    sliced = plan.choose_slices(max_sliced=6, log2_target=0)
+    amp = plan.run_sliced(sliced, batch=16)
+    ref = O.statevector(16, g)[O.amplitude_index(bits)]
+    assert abs(amp - ref) / 2.0 ** -8 < TOL[prec]
+    plan.close()
+    be.close()
+
+
+def test_plan_rejects_bad_input(pq):
+    from pqgb300 import _lib as L
+
+    be = pq.GB300Backend(pq.PREC_C64)
+    net, _ = open_net(pq, be, 2, 2, 2, seed=1)
+    plan = pq.NetworkPlan(net, planner="greedy")
+    bad = list(plan.steps)
+    bad[0] = bad[1]
+    with pytest.raises(L.PQError):
+        pq.NetworkPlan(net, steps=bad)
+    # a leaf replaced by a tensor of the wrong size
+    first = net.nodes[plan.leaves[0]].data_label
+    be.save_tensor_data(first, np.ones((3,)))
+    with pytest.raises(L.PQError) as e:
+        plan.execute()
+    assert e.value.code == L.PQ_ERR_INVALID
+    plan.close()
+    be.close()
