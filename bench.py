@@ -448,6 +448,9 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
                                        "sample": "the same amplitude, all slices, complex128 FP64 kernels"}
             extra["speedup_vs_plain_fp64"] = value / extra["plain_fp64_gpu"]["value"]
             extra["rel_err_vs_fp64"] = abs(result - a64) / abs(a64)
+            # the same error relative to the amplitude scale 2^(-n/2) (amplitudes
+            # of random circuits are Porter-Thomas distributed around it)
+            extra["err_vs_fp64_over_2^-n/2"] = abs(result - a64) / 2.0 ** (-rows * cols / 2)
             w64["plan"].close()
             w64["be"].close()
         extra["amplitude"] = [float(np.real(result)), float(np.imag(result))]

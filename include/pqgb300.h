@@ -75,6 +75,11 @@ int pq_ctx_sync(pq_ctx* ctx);
  * beyond the cap fail with PQ_ERR_OOM (host-side fault injection). */
 int pq_ctx_set_mem_cap(pq_ctx* ctx, int64_t bytes);
 int pq_ctx_mem_in_use(pq_ctx* ctx, int64_t* bytes);
+/* Precision policy of the complex64 modes: tensors of at most `n` elements
+ * are stored (and their contractions accumulated) in complex128, larger ones
+ * in complex64 (default n = 65536; 0 stores everything as complex64).
+ * Applies to tensors created afterwards. */
+int pq_ctx_set_small_elems(pq_ctx* ctx, int64_t n);
 /* Number of kernels this context has launched so far. */
 int pq_ctx_launch_count(pq_ctx* ctx, int64_t* count);
 /* The CUDA stream of the context (a cudaStream_t), for callers that order

@@ -63,6 +63,7 @@ SIGNATURES = [
     ("pq_ctx_set_mem_cap", C.c_int, [vp, C.c_int64]),
     ("pq_ctx_mem_in_use", C.c_int, [vp, i64p]),
     ("pq_ctx_launch_count", C.c_int, [vp, i64p]),
+    ("pq_ctx_set_small_elems", C.c_int, [vp, C.c_int64]),
     ("pq_ctx_stream", C.c_int, [vp, C.POINTER(vp)]),
     ("pq_save_tensor_data", C.c_int, [vp, C.c_int64, C.c_int, i64p, vp, C.c_int]),
     ("pq_load_tensor_data", C.c_int, [vp, C.c_int64, vp, C.c_int64, C.c_int]),

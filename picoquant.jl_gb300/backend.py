@@ -53,11 +53,15 @@ class GB300Backend:
 
     ``precision`` selects storage and arithmetic (the role of the element type
     ``T`` of ``InteractiveBackend{T}``): PREC_C128 (ComplexF64, FP64 math),
-    PREC_C64 (ComplexF32, FP32 math), PREC_3XTF32 / PREC_3XBF16 (ComplexF32
-    storage, split-precision tensor-core products for large pairs).
+    PREC_C64 (ComplexF32 storage and FP32 math for large tensors),
+    PREC_3XTF32 / PREC_3XBF16 (as PREC_C64, with split-precision tensor-core
+    products for large pairs).  In the complex64 modes tensors of at most
+    ``small_elems`` elements (default 65536) stay complex128: gate tensors and
+    small intermediates cost nothing in time, and rounding them would dominate
+    the error of the final amplitudes.
     """
 
-    def __init__(self, precision: int = L.PREC_C64, device: int = 0):
+    def __init__(self, precision: int = L.PREC_C64, device: int = 0, small_elems: int | None = None):
         self.lib = L.lib()
         h = C.c_void_p()
         rc = self.lib.pq_ctx_create(device, precision, C.byref(h))
@@ -65,6 +69,8 @@ class GB300Backend:
             raise L.PQError(rc, f"pq_ctx_create(device={device}, precision={precision}) failed")
         self.ctx = h
         self.precision = precision
+        if small_elems is not None:
+            self._check(self.lib.pq_ctx_set_small_elems(self.ctx, int(small_elems)), "set_small_elems")
         self.metrics = Metrics()
         self._ids: dict[str, int] = {}
         self._next = 1
@@ -117,14 +123,15 @@ class GB300Backend:
     def save_tensor_data(self, label, data):
         """src/backends/interactive.jl:32-36."""
         a = np.asarray(data)
+        shape = a.shape  # (asfortranarray turns a 0-d array into shape (1,))
         if a.dtype == np.complex64:
             a = np.asfortranarray(a)
             dt = L.PQ_C64
         else:
             a = np.asfortranarray(a, dtype=np.complex128)
             dt = L.PQ_C128
-        dims = L.arr(C.c_int64, a.shape)
-        rc = self.lib.pq_save_tensor_data(self.ctx, self.id_of(label), a.ndim, dims,
+        dims = L.arr(C.c_int64, shape)
+        rc = self.lib.pq_save_tensor_data(self.ctx, self.id_of(label), len(shape), dims,
                                           a.ctypes.data_as(C.c_void_p), dt)
         self._check(rc, f"save_tensor_data({label})")
 

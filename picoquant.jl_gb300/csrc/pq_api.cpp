@@ -67,11 +67,27 @@ static void put_entry(Ctx* ctx, int64_t id, Tensor&& t) {
   }
 }
 
-int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, Tensor& t) {
+int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, int dtype, Tensor& t) {
   t.dims = dims;
   t.size = prod(dims);
-  t.bytes = (size_t)t.size * ctx->elem;
+  t.dtype = dtype;
+  t.bytes = (size_t)t.size * elem_bytes(dtype);
   return dev_alloc(ctx, t.bytes, &t.ptr);
+}
+
+// Convert n complex elements between host representations.
+static void convert_host(const void* src, int sdt, void* dst, int ddt, int64_t n) {
+  if (sdt == ddt) {
+    std::memcpy(dst, src, (size_t)n * elem_bytes(sdt));
+  } else if (sdt == PQ_C128) {
+    const double* s = (const double*)src;
+    float* o = (float*)dst;
+    for (int64_t i = 0; i < 2 * n; ++i) o[i] = (float)s[i];
+  } else {
+    const float* s = (const float*)src;
+    double* o = (double*)dst;
+    for (int64_t i = 0; i < 2 * n; ++i) o[i] = (double)s[i];
+  }
 }
 
 int check_status(Ctx* ctx) {
@@ -106,7 +122,6 @@ int pq_ctx_create(int device, int precision, pq_ctx** out) {
   Ctx* ctx = &c->impl;
   ctx->device = device;
   ctx->precision = precision;
-  ctx->elem = precision == PQ_PREC_C128 ? 16 : 8;
   e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -201,25 +216,15 @@ int pq_save_tensor_data(pq_ctx* c, int64_t id, int rank, const int64_t* dims, co
   for (auto x : d)
     if (x < 1) return fail(ctx, PQ_ERR_INVALID, "save_tensor_data: extents must be >= 1");
   Tensor t;
-  int st = alloc_tensor(ctx, d, t);
+  int st = alloc_tensor(ctx, d, storage_dtype(ctx, prod(d)), t);
   if (st) return st;
-  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
   cudaError_t e;
-  if (host_elem == ctx->elem) {
+  if (t.dtype == dtype) {
     e = cudaMemcpyAsync(t.ptr, data, t.bytes, cudaMemcpyHostToDevice, ctx->stream);
   } else {
-    // convert on the host (gate tensors are small; large states should be
-    // uploaded in the storage type)
+    // convert on the host (large states should be uploaded in the storage type)
     std::vector<unsigned char> tmp(t.bytes);
-    if (dtype == PQ_C128) {
-      const double* s = (const double*)data;
-      float* o = (float*)tmp.data();
-      for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (float)s[i];
-    } else {
-      const float* s = (const float*)data;
-      double* o = (double*)tmp.data();
-      for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (double)s[i];
-    }
+    convert_host(data, dtype, tmp.data(), t.dtype, t.size);
     e = cudaMemcpyAsync(t.ptr, tmp.data(), t.bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   }
@@ -238,9 +243,8 @@ int pq_load_tensor_data(pq_ctx* c, int64_t id, void* dst, int64_t n_elems, int d
   const Tensor& t = it->second;
   if (!dst || n_elems < t.size) return fail(ctx, PQ_ERR_INVALID, "load_tensor_data: destination too small");
   if (dtype != PQ_C64 && dtype != PQ_C128) return fail(ctx, PQ_ERR_INVALID, "load_tensor_data: bad dtype");
-  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
   cudaError_t e;
-  if (host_elem == ctx->elem) {
+  if (t.dtype == dtype) {
     e = cudaMemcpyAsync(dst, t.ptr, t.bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "load_tensor_data download");
     return check_status(ctx);
@@ -250,15 +254,7 @@ int pq_load_tensor_data(pq_ctx* c, int64_t id, void* dst, int64_t n_elems, int d
   if (e != cudaSuccess) return cuda_fail(ctx, e, "load_tensor_data download");
   int st = check_status(ctx);
   if (st) return st;
-  if (ctx->elem == 8) {
-    const float* s = (const float*)tmp.data();
-    double* o = (double*)dst;
-    for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = s[i];
-  } else {
-    const double* s = (const double*)tmp.data();
-    float* o = (float*)dst;
-    for (int64_t i = 0; i < 2 * t.size; ++i) o[i] = (float)s[i];
-  }
+  convert_host(tmp.data(), t.dtype, dst, dtype, t.size);
   return PQ_OK;
 }
 
@@ -292,7 +288,7 @@ int pq_save_output(pq_ctx* c, int64_t node, int64_t name) {
   if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "save_output: no tensor " + std::to_string(node));
   if (node == name) return PQ_OK;
   Tensor t;
-  int st = alloc_tensor(ctx, it->second.dims, t);
+  int st = alloc_tensor(ctx, it->second.dims, it->second.dtype, t);
   if (st) return st;
   cudaError_t e = cudaMemcpyAsync(t.ptr, it->second.ptr, t.bytes, cudaMemcpyDeviceToDevice, ctx->stream);
   if (e != cudaSuccess) {
@@ -322,7 +318,7 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
   if (!analyse_pair(la, A.dims, lb, B.dims, lc, ctx->precision, pp, err))
     return fail(ctx, PQ_ERR_INVALID, "contract_tensors: " + err);
   Tensor C;
-  int st = alloc_tensor(ctx, pp.c_dims, C);
+  int st = alloc_tensor(ctx, pp.c_dims, storage_dtype(ctx, pp.csize), C);
   if (st) return st;
   cudaError_t e;
   void* scratch = nullptr;
@@ -334,13 +330,14 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
       free_tensor(ctx, C);
       return st;
     }
-    e = launch_tc(ctx->precision, A.ptr, B.ptr, C.ptr, pp.m, scratch, sbytes, ctx->stream);
+    e = launch_tc(ctx->precision, A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, scratch, sbytes,
+                  ctx->stream);
     ctx->launches += 4;
   } else if (pp.kclass == KC_GEMM) {
-    e = launch_gemm(ctx->precision, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
+    e = launch_gemm(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
     ctx->launches += 1;
   } else {
-    e = launch_generic(ctx->precision, A.ptr, B.ptr, C.ptr, pp.g, ctx->stream);
+    e = launch_generic(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.g, ctx->stream);
     ctx->launches += 1;
   }
   if (scratch) dev_free(ctx, scratch, sbytes);
@@ -379,9 +376,9 @@ int pq_permute_tensor(pq_ctx* c, int64_t id, const int32_t* perm1, int rank) {
   if (!analyse_pair(la, T.dims, {}, {}, lc, ctx->precision, pp, err))
     return fail(ctx, PQ_ERR_INVALID, "permute_tensor: " + err);
   Tensor O;
-  int st = alloc_tensor(ctx, pp.c_dims, O);
+  int st = alloc_tensor(ctx, pp.c_dims, T.dtype, O);
   if (st) return st;
-  cudaError_t e = launch_permute(ctx->precision, T.ptr, 0, O.ptr, pp.g, ctx->stream);
+  cudaError_t e = launch_permute(T.dtype, O.dtype, T.ptr, 0, O.ptr, pp.g, ctx->stream);
   ctx->launches += 1;
   if (e != cudaSuccess) {
     free_tensor(ctx, O);
@@ -424,17 +421,9 @@ int pq_view_tensor(pq_ctx* c, int64_t view_id, int64_t node, int bond_idx1, int6
   const int ax = bond_idx1 - 1;
   if (ax < 0 || ax >= r || lo1 < 1 || hi1 < lo1 || hi1 > T.dims[ax])
     return fail(ctx, PQ_ERR_INVALID, "view_tensor: bad bond index or range");
-  std::vector<int> la(r);
-  for (int i = 0; i < r; ++i) la[i] = i;
-  PairPlan pp;
-  std::string err;
   std::vector<int64_t> vd = T.dims;
   vd[ax] = hi1 - lo1 + 1;
-  // analyse as a permutation of a tensor with the narrowed extent (the input
-  // strides are those of the full tensor)
-  if (!analyse_pair(la, T.dims, {}, {}, la, ctx->precision, pp, err))
-    return fail(ctx, PQ_ERR_INVALID, "view_tensor: " + err);
-  // rebuild the descriptor without merging across the narrowed mode
+  // copy descriptor: narrowed extents, strides of the full tensor
   GenericDesc g;
   std::memset(&g, 0, sizeof(g));
   int64_t stride = 1, size = 1;
@@ -453,9 +442,9 @@ int pq_view_tensor(pq_ctx* c, int64_t view_id, int64_t node, int bond_idx1, int6
   int64_t base = (lo1 - 1);
   for (int i = 0; i < ax; ++i) base *= T.dims[i];
   Tensor O;
-  int st = alloc_tensor(ctx, vd, O);
+  int st = alloc_tensor(ctx, vd, T.dtype, O);
   if (st) return st;
-  cudaError_t e = launch_permute(ctx->precision, T.ptr, base, O.ptr, g, ctx->stream);
+  cudaError_t e = launch_permute(T.dtype, O.dtype, T.ptr, base, O.ptr, g, ctx->stream);
   ctx->launches += 1;
   if (e != cudaSuccess) {
     free_tensor(ctx, O);
@@ -475,37 +464,34 @@ int pq_gather_elements(pq_ctx* c, int64_t id, const int64_t* idx, int64_t n, voi
   for (int64_t i = 0; i < n; ++i)
     if (idx[i] < 0 || idx[i] >= T.size) return fail(ctx, PQ_ERR_INVALID, "gather_elements: index out of range");
   if (n == 0) return PQ_OK;
+  const size_t eb = elem_bytes(T.dtype);
   void* d_idx = nullptr;
   void* d_out = nullptr;
   int st = dev_alloc(ctx, (size_t)n * 8, &d_idx);
   if (st) return st;
-  st = dev_alloc(ctx, (size_t)n * ctx->elem, &d_out);
+  st = dev_alloc(ctx, (size_t)n * eb, &d_out);
   if (st) {
     dev_free(ctx, d_idx, (size_t)n * 8);
     return st;
   }
   cudaError_t e = cudaMemcpyAsync(d_idx, idx, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_gather(ctx->precision, T.ptr, (const int64_t*)d_idx, n, d_out, ctx->stream);
+  if (e == cudaSuccess) e = launch_gather(T.dtype, T.ptr, (const int64_t*)d_idx, n, d_out, ctx->stream);
   ctx->launches += 1;
-  std::vector<unsigned char> tmp((size_t)n * ctx->elem);
+  std::vector<unsigned char> tmp((size_t)n * eb);
   if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d_out, tmp.size(), cudaMemcpyDeviceToHost, ctx->stream);
   dev_free(ctx, d_idx, (size_t)n * 8);
-  dev_free(ctx, d_out, (size_t)n * ctx->elem);
+  dev_free(ctx, d_out, (size_t)n * eb);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gather_elements");
   st = check_status(ctx);
   if (st) return st;
-  const size_t host_elem = dtype == PQ_C128 ? 16 : 8;
-  if (host_elem == ctx->elem) {
-    std::memcpy(out, tmp.data(), tmp.size());
-  } else if (ctx->elem == 8) {
-    const float* s = (const float*)tmp.data();
-    double* o = (double*)out;
-    for (int64_t i = 0; i < 2 * n; ++i) o[i] = s[i];
-  } else {
-    const double* s = (const double*)tmp.data();
-    float* o = (float*)out;
-    for (int64_t i = 0; i < 2 * n; ++i) o[i] = (float)s[i];
-  }
+  convert_host(tmp.data(), T.dtype, out, dtype, n);
+  return PQ_OK;
+}
+
+int pq_ctx_set_small_elems(pq_ctx* c, int64_t n) {
+  CTX_OR_FAIL(c);
+  if (n < 0) return fail(ctx, PQ_ERR_INVALID, "set_small_elems: negative threshold");
+  ctx->small_elems = n;
   return PQ_OK;
 }
 

@@ -75,6 +75,7 @@ std::vector<int> symdiff_labels(const std::vector<int>& la, const std::vector<in
 
 struct Tensor {
   void* ptr = nullptr;
+  int dtype = PQ_C128;  // storage element type
   std::vector<int64_t> dims;
   int64_t size = 1;
   size_t bytes = 0;
@@ -92,7 +93,18 @@ struct Ctx {
   int64_t mem_cap = 0;
   int64_t mem_in_use = 0;
   int64_t launches = 0;
+  // Mixed-precision contexts store tensors of at most this many elements as
+  // complex128 (gates, per-qubit tensors: cheap, and their rounding would
+  // dominate the error) and larger ones as complex64.
+  int64_t small_elems = int64_t(1) << 16;
 };
+
+inline size_t elem_bytes(int dt) { return dt == PQ_C128 ? 16 : 8; }
+// Storage type of a tensor of `n` elements in this context.
+inline int storage_dtype(const Ctx* ctx, int64_t n) {
+  if (ctx->precision == PQ_PREC_C128) return PQ_C128;
+  return n <= ctx->small_elems ? PQ_C128 : PQ_C64;
+}
 
 // Status helpers: set the context error and return the code.
 int fail(Ctx* ctx, int code, const std::string& msg);
@@ -102,32 +114,33 @@ int cuda_fail(Ctx* ctx, cudaError_t e, const char* what);
 int dev_alloc(Ctx* ctx, size_t bytes, void** p);
 void dev_free(Ctx* ctx, void* p, size_t bytes);
 
-// ---- kernel launchers (pq_kernels.cu) ----------------------------------
-// All launches are asynchronous on `stream` and return the launch error.
-cudaError_t launch_generic(int precision, const void* A, const void* B, void* C,
+// ---- kernel launchers (pq_kernels.cu, pq_gemm.cu) -------------------------
+// Element types are PQ_C64 / PQ_C128 per operand.  All launches are
+// asynchronous on `stream` and return the launch error.
+cudaError_t launch_generic(int ta, int tb, int tc, const void* A, const void* B, void* C,
                            const GenericDesc& d, cudaStream_t stream);
-cudaError_t launch_gemm(int precision, const void* A, const void* B, void* C,
+cudaError_t launch_gemm(int ta, int tb, int tc, const void* A, const void* B, void* C,
                         const GemmDesc& d, cudaStream_t stream);
 // out[c] = in[base + sum_i idx_i * stride_i] over `d` (uses csa as input
-// strides, C storage column-major).
-cudaError_t launch_permute(int precision, const void* in, int64_t base, void* out,
+// strides, C storage column-major), converting tin -> tout.
+cudaError_t launch_permute(int tin, int tout, const void* in, int64_t base, void* out,
                            const GenericDesc& d, cudaStream_t stream);
-cudaError_t launch_gather(int precision, const void* in, const int64_t* d_idx, int64_t n,
+cudaError_t launch_gather(int dt, const void* in, const int64_t* d_idx, int64_t n,
                           void* out, cudaStream_t stream);
 // Batched leaf gather for slicing: out[x + xs*b] = in[x_off(x) + slice_off(s0+b)]
 // for b < nb, where x runs over `d` (csa = input strides of the kept modes)
 // and the slice offset is the mixed-radix digits of (s0+b) over the sliced
 // dims times their strides in `in`.  Entries with s0+b >= s_end are zero.
-cudaError_t launch_slice_gather(int precision, const void* in, void* out, const GenericDesc& d,
+cudaError_t launch_slice_gather(int dt, const void* in, void* out, const GenericDesc& d,
                                 int nsl, const int64_t* sl_dim, const int64_t* sl_stride,
                                 int64_t s0, int64_t nb, int64_t s_end, cudaStream_t stream);
 // Neumaier FP64 sum over the batch axis: acc[e] += sum_b X[e + n*b].
-cudaError_t launch_slice_sum(int precision, const void* X, int64_t n, int64_t nb,
+cudaError_t launch_slice_sum(int dt, const void* X, int64_t n, int64_t nb,
                              double* acc, double* comp, cudaStream_t stream);
 // Split-precision tensor-core GEMM-class contraction (pq_tc.cu).  Returns
 // cudaErrorNotSupported when the shape is not eligible.
-cudaError_t launch_tc(int precision, const void* A, const void* B, void* C, const GemmDesc& d,
-                      void* scratch, size_t scratch_bytes, cudaStream_t stream);
+cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C,
+                      const GemmDesc& d, void* scratch, size_t scratch_bytes, cudaStream_t stream);
 size_t tc_scratch_bytes(int precision, const GemmDesc& d);
 bool tc_eligible(int precision, const GemmDesc& d);
 

@@ -22,7 +22,7 @@
 #include "pq_internal.h"
 
 namespace pq {
-int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, Tensor& t);
+int alloc_tensor(Ctx* ctx, const std::vector<int64_t>& dims, int dtype, Tensor& t);
 int check_status(Ctx* ctx);
 }  // namespace pq
 
@@ -37,12 +37,14 @@ struct Step {
   size_t bytes = 0;
   bool batched = false;
   bool is_copy = false;  // single-leaf network: result = permuted copy of x
+  int ta = PQ_C128, tb = PQ_C128, tc = PQ_C128;  // storage types of A, B, C
 };
 
 struct Compiled {
   int nleaves = 0;
   std::vector<std::vector<int>> labels;    // per SSA value
   std::vector<std::vector<int64_t>> dims;  // per SSA value
+  std::vector<int> dt;                     // storage type per SSA value
   std::vector<Step> steps;                 // in execution order
   std::vector<int> order;                  // steps' original indices
   size_t arena_bytes = 0;
@@ -57,7 +59,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Liveness-driven first-fit arena assignment.  `pinned[v]` values are never
 // released once computed (used for sliced execution).
-void assign_arena(Compiled& cp, size_t elem, const std::vector<char>& pinned) {
+void assign_arena(Compiled& cp, const std::vector<char>& pinned) {
   const int nv = (int)cp.labels.size();
   std::vector<int> last_use(nv, -1);
   for (int i = 0; i < (int)cp.steps.size(); ++i) {
@@ -137,6 +139,7 @@ struct pq_plan {
   std::vector<size_t> sl_leaf_off;         // offsets of gathered leaves in arena (after scp arena)
   std::vector<GenericDesc> sl_leaf_desc;
   std::vector<std::vector<int64_t>> sl_leaf_sdim, sl_leaf_sstride;
+  std::vector<int> sl_leaf_dt;             // storage type of each gathered leaf
   size_t sl_total_bytes = 0;
   double* d_acc = nullptr;  // 2*n complex sum + 2*n compensation
   int64_t out_elems = 0;
@@ -145,16 +148,19 @@ struct pq_plan {
 namespace {
 
 // Compile `steps` (SSA pairs in execution order) for the given leaf labels.
-bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& leaf_labels,
+bool compile(const Ctx* ctx, const std::vector<std::vector<int>>& leaf_labels,
              const std::vector<int64_t>& label_dims, const std::vector<int>& steps,
              const std::vector<int>& out_labels, const std::vector<int>& exec_order,
-             const std::vector<char>* batched_leaf, Compiled& cp, std::string& err) {
+             const std::vector<char>* batched_leaf, Compiled& cp, std::string& err,
+             const std::vector<int>* leaf_dt = nullptr) {
   cp = Compiled();
+  const int precision = ctx->precision;
   const int nl = (int)leaf_labels.size();
   const int ns = (int)steps.size() / 2;
   cp.nleaves = nl;
   cp.labels.assign(nl + std::max(ns, 1), {});
   cp.dims.assign(nl + std::max(ns, 1), {});
+  cp.dt.assign(nl + std::max(ns, 1), PQ_C128);
   for (int i = 0; i < nl; ++i) {
     cp.labels[i] = leaf_labels[i];
     for (int l : leaf_labels[i]) {
@@ -164,6 +170,9 @@ bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& le
       }
       cp.dims[i].push_back(label_dims[l]);
     }
+    int64_t sz = 1;
+    for (auto d : cp.dims[i]) sz *= d;
+    cp.dt[i] = leaf_dt ? (*leaf_dt)[i] : storage_dtype(ctx, sz);
   }
   for (int l : out_labels)
     if (l < 0 || l >= (int)label_dims.size()) {
@@ -197,7 +206,10 @@ bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& le
       return false;
     }
     if (!analyse_pair(la, cp.dims[0], {}, {}, out_labels, precision, s.pp, err)) return false;
-    s.bytes = (size_t)s.pp.csize * elem;
+    s.ta = s.tb = cp.dt[0];
+    s.tc = cp.dt[0];
+    s.bytes = (size_t)s.pp.csize * elem_bytes(s.tc);
+    cp.dt[nl] = s.tc;
     cp.steps.push_back(s);
     cp.order.push_back(0);
     cp.labels[nl] = out_labels;
@@ -206,7 +218,7 @@ bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& le
     cp.max_elems = s.pp.csize;
     cp.launches = 1;
     std::vector<char> pinned(nl + 1, 0);
-    assign_arena(cp, elem, pinned);
+    assign_arena(cp, pinned);
     return true;
   }
   // first pass in given order to define labels (must be a valid SSA program)
@@ -254,7 +266,11 @@ bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& le
       err = "step " + std::to_string(i) + ": " + err;
       return false;
     }
-    s.bytes = (size_t)s.pp.csize * elem;
+    s.ta = cp.dt[x];
+    s.tb = cp.dt[y];
+    s.tc = storage_dtype(ctx, s.pp.csize);
+    cp.dt[r] = s.tc;
+    s.bytes = (size_t)s.pp.csize * elem_bytes(s.tc);
     cp.labels[r] = lr;
     cp.dims[r] = s.pp.c_dims;
     for (int l : lr) cnt[l]++;
@@ -288,21 +304,22 @@ bool compile(int precision, size_t elem, const std::vector<std::vector<int>>& le
         for (int v : {s.x, s.y})
           if (v >= nl && !batched[v]) pinned[v] = 1;
   }
-  assign_arena(cp, elem, pinned);
+  assign_arena(cp, pinned);
   return true;
 }
 
 cudaError_t run_step(pq_plan* p, const Step& s, const void* A, const void* B, void* C) {
   Ctx* ctx = p->ctx;
   ctx->launches += (s.pp.kclass == KC_TC) ? 4 : 1;
-  if (s.is_copy) return launch_permute(ctx->precision, A, 0, C, s.pp.g, ctx->stream);
+  if (s.is_copy) return launch_permute(s.ta, s.tc, A, 0, C, s.pp.g, ctx->stream);
   switch (s.pp.kclass) {
     case KC_TC:
-      return launch_tc(ctx->precision, A, B, C, s.pp.m, p->scratch, p->scratch_cap, ctx->stream);
+      return launch_tc(ctx->precision, s.ta, s.tb, s.tc, A, B, C, s.pp.m, p->scratch, p->scratch_cap,
+                       ctx->stream);
     case KC_GEMM:
-      return launch_gemm(ctx->precision, A, B, C, s.pp.m, ctx->stream);
+      return launch_gemm(s.ta, s.tb, s.tc, A, B, C, s.pp.m, ctx->stream);
     default:
-      return launch_generic(ctx->precision, A, B, C, s.pp.g, ctx->stream);
+      return launch_generic(s.ta, s.tb, s.tc, A, B, C, s.pp.g, ctx->stream);
   }
 }
 
@@ -357,6 +374,9 @@ int leaf_pointers(pq_plan* p, const int64_t* leaf_ids, std::vector<const void*>&
       return fail(ctx, PQ_ERR_INVALID, "plan: tensor " + std::to_string(leaf_ids[i]) + " has " +
                                            std::to_string(t.size) + " elements, leaf " + std::to_string(i) +
                                            " needs " + std::to_string(want));
+    if (t.dtype != p->cp.dt[i])
+      return fail(ctx, PQ_ERR_INVALID, "plan: tensor " + std::to_string(leaf_ids[i]) +
+                                           " has a different storage type than the plan expects");
     ptrs[i] = t.ptr;
   }
   return PQ_OK;
@@ -390,7 +410,7 @@ int store_result(pq_plan* p, int64_t out_id) {
   Ctx* ctx = p->ctx;
   const auto& dims = p->cp.dims[p->cp.result_ssa];
   Tensor t;
-  int st = alloc_tensor(ctx, dims, t);
+  int st = alloc_tensor(ctx, dims, p->cp.dt[p->cp.result_ssa], t);
   if (st) return st;
   cudaError_t e = cudaMemcpyAsync(t.ptr, (const char*)p->arena + result_off(p->cp), t.bytes,
                                   cudaMemcpyDeviceToDevice, ctx->stream);
@@ -448,7 +468,7 @@ int pq_plan_create(pq_ctx* c, int n_leaves, const int32_t* leaf_ranks, const int
   p->steps_in.assign(steps, steps + 2 * n_steps);
   p->out_labels.assign(out_labels, out_labels + n_out);
   std::string err;
-  if (!compile(ctx->precision, ctx->elem, p->leaf_labels, p->label_dims, p->steps_in, p->out_labels, {}, nullptr,
+  if (!compile(ctx, p->leaf_labels, p->label_dims, p->steps_in, p->out_labels, {}, nullptr,
                p->cp, err)) {
     delete p;
     return fail(ctx, PQ_ERR_INVALID, "plan_create: " + err);
@@ -569,9 +589,9 @@ int pq_plan_profile(pq_plan* p, const int64_t* leaf_ids, int64_t out_id, float* 
 
 int pq_plan_step_features(pq_plan* p, double* feats) {
   if (!p || !feats) return PQ_ERR_INVALID;
-  const double elem = (double)p->ctx->elem;
   for (size_t i = 0; i < p->cp.steps.size(); ++i) {
     const PairPlan& q = p->cp.steps[i].pp;
+    const Step& s = p->cp.steps[i];
     double* f = feats + 8 * p->cp.order[i];
     f[0] = std::log2((double)q.asize);
     f[1] = std::log2((double)q.bsize);
@@ -580,7 +600,8 @@ int pq_plan_step_features(pq_plan* p, double* feats) {
     f[4] = std::log2((double)q.run_a);
     f[5] = std::log2((double)q.run_b);
     f[6] = (double)q.kclass;
-    f[7] = elem * (double)(q.asize + q.bsize + q.csize);
+    f[7] = (double)elem_bytes(s.ta) * q.asize + (s.is_copy ? 0.0 : (double)elem_bytes(s.tb) * q.bsize) +
+           (double)elem_bytes(s.tc) * q.csize;
   }
   return PQ_OK;
 }
@@ -618,6 +639,7 @@ int prepare_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int3
     p->sl_leaf_desc.clear();
     p->sl_leaf_sdim.clear();
     p->sl_leaf_sstride.clear();
+    p->sl_leaf_dt.clear();
     for (int i = 0; i < p->nleaves; ++i) {
       const auto& lab = p->leaf_labels[i];
       bool hit = false;
@@ -659,6 +681,7 @@ int prepare_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int3
       p->sl_leaf_desc.push_back(g);
       p->sl_leaf_sdim.push_back(sd);
       p->sl_leaf_sstride.push_back(ss);
+      p->sl_leaf_dt.push_back(p->cp.dt[i]);
     }
     std::vector<int> outl = p->out_labels;
     outl.push_back(beta);
@@ -674,13 +697,13 @@ int prepare_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int3
     std::vector<int> order = first;
     order.insert(order.end(), second.begin(), second.end());
     std::string err;
-    if (!compile(ctx->precision, ctx->elem, ll, ldims, p->steps_in, outl, order, &bl, p->scp, err))
+    if (!compile(ctx, ll, ldims, p->steps_in, outl, order, &bl, p->scp, err, &p->cp.dt))
       return fail(ctx, PQ_ERR_INVALID, "run_sliced: " + err);
     // gathered leaf buffers after the arena
     size_t off = align_up(p->scp.arena_bytes, 256);
     for (size_t j = 0; j < p->sl_leaf_desc.size(); ++j) {
       p->sl_leaf_off.push_back(off);
-      off += align_up((size_t)p->sl_leaf_desc[j].csize * batch * ctx->elem, 256);
+      off += align_up((size_t)p->sl_leaf_desc[j].csize * batch * elem_bytes(p->sl_leaf_dt[j]), 256);
     }
     p->sl_total_bytes = off;
     p->sl_labels = S;
@@ -699,7 +722,7 @@ cudaError_t gather_batch(pq_plan* p, const std::vector<const void*>& ptrs, int64
   for (int i = 0; i < p->nleaves; ++i) {
     int j = p->sl_leaf_of[i];
     if (j < 0) continue;
-    cudaError_t e = launch_slice_gather(ctx->precision, ptrs[i], (char*)p->arena + p->sl_leaf_off[j],
+    cudaError_t e = launch_slice_gather(p->sl_leaf_dt[j], ptrs[i], (char*)p->arena + p->sl_leaf_off[j],
                                         p->sl_leaf_desc[j], (int)p->sl_labels.size(), p->sl_leaf_sdim[j].data(),
                                         p->sl_leaf_sstride[j].data(), s0, p->sl_batch, s0 + nb, ctx->stream);
     ctx->launches++;
@@ -748,7 +771,7 @@ int pq_plan_run_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const 
     if (eg != cudaSuccess) return cuda_fail(ctx, eg, "slice gather");
     st = launch_all(p, p->scp, lp, true, false);
     if (st) return st;
-    cudaError_t e = launch_slice_sum(ctx->precision, (const char*)p->arena + res_off, oe, nb, p->d_acc,
+    cudaError_t e = launch_slice_sum(p->scp.dt[p->scp.result_ssa], (const char*)p->arena + res_off, oe, nb, p->d_acc,
                                      p->d_acc + 2 * oe, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "slice sum");
@@ -779,7 +802,6 @@ int pq_plan_profile_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, co
     cudaEventRecord(ev[i + 1], ctx->stream);
   }
   if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
-  const double elem = (double)ctx->elem;
   for (size_t i = 0; i < n; ++i) {
     float t = 0;
     if (e == cudaSuccess) cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
@@ -795,7 +817,9 @@ int pq_plan_profile_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, co
     f[4] = std::log2((double)q.run_a);
     f[5] = std::log2((double)q.run_b);
     f[6] = (double)q.kclass;
-    f[7] = elem * (double)(q.asize + q.bsize + q.csize);
+    const Step& s = cp.steps[i];
+    f[7] = (double)elem_bytes(s.ta) * q.asize + (s.is_copy ? 0.0 : (double)elem_bytes(s.tb) * q.bsize) +
+           (double)elem_bytes(s.tc) * q.csize;
   }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "profile sliced");

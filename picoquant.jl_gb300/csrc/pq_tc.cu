@@ -16,9 +16,12 @@ size_t tc_scratch_bytes(int precision, const GemmDesc& d) {
   return 0;
 }
 
-cudaError_t launch_tc(int precision, const void* A, const void* B, void* C, const GemmDesc& d, void* scratch,
-                      size_t scratch_bytes, cudaStream_t stream) {
+cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C,
+                      const GemmDesc& d, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
   (void)precision;
+  (void)ta;
+  (void)tb;
+  (void)tc;
   (void)A;
   (void)B;
   (void)C;

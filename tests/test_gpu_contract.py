@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {0: 1e-12, 1: 2e-6}
+TOL = {0: 1e-12, 1: 2e-6, "c64all": 2e-6}
 
 
 def rel_err(a, b):
@@ -36,9 +36,12 @@ def make_case(rng, n_common, n_a, n_b, dim_choices=(1, 2, 3, 4), big=False):
     return A, ia, B, ib
 
 
-@pytest.fixture(params=[0, 1], ids=["c128", "c64"])
+@pytest.fixture(params=[0, 1, "c64all"], ids=["c128", "c64", "c64all"])
 def backend(request, pq):
-    be = pq.GB300Backend(precision=request.param)
+    if request.param == "c64all":  # every tensor stored as complex64
+        be = pq.GB300Backend(precision=1, small_elems=0)
+    else:
+        be = pq.GB300Backend(precision=request.param)
     yield be
     be.close()
 
