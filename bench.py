@@ -131,6 +131,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="grid6x6_d16_sliced", choices=["grid6x6_d16_sliced", "grid4x5_d12_amps"])
+    ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
+    ap.add_argument("--cols", type=int, default=6)
+    ap.add_argument("--depth", type=int, default=16)
     ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "3xbf16", "c128"])
     ap.add_argument("--batch", type=int, default=0, help="slices per launch (0: sized from memory)")
     ap.add_argument("--cpu-log2", type=float, default=31.0, help="log2 complex MACs of the CPU sample")
@@ -157,7 +160,7 @@ def run_reference(args):
 
     pq = g.load_package()
     cores = os.cpu_count()
-    rows, cols, depth = (6, 6, 16) if args.workload == "grid6x6_d16_sliced" else (4, 5, 12)
+    rows, cols, depth = (args.rows, args.cols, args.depth) if args.workload == "grid6x6_d16_sliced" else (4, 5, 12)
     val, sample = cpu_sample(pq, O, args, rows, cols, depth)
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "amplitudes/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -316,7 +319,7 @@ def run_gb300(args, world, rank):
     precision = prec_map[prec_name]
 
     if args.workload == "grid6x6_d16_sliced":
-        rows, cols, depth = 6, 6, 16
+        rows, cols, depth = args.rows, args.cols, args.depth
         w = build_sliced(pq, precision, rows, cols, depth, rank=rank, target=args.slice_target)
         be, plan, sliced = w["be"], w["plan"], w["sliced"]
         if args.batch <= 0:
