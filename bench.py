@@ -457,8 +457,6 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
             w64["plan"].close()
             w64["be"].close()
         extra["amplitude"] = [float(np.real(result)), float(np.imag(result))]
-        w64["plan"].close()
-        w64["be"].close()
         extra["plan"] = {"planner": w["planner"], "cmacs_unsliced": w["cmacs"], "max_elems_unsliced": w["max_elems"],
                          "sliced_bonds": len(sliced), "planning_s": w["t_plan"]}
     else:

@@ -219,6 +219,40 @@ int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t
                           const int32_t* steps, int n_out, const int32_t* out_labels,
                           int max_sliced, double log2_target, int32_t* sliced, int* n_sliced);
 
+/* ---- learned cost model ------------------------------------------------------
+ * No counterpart in the reference (its planners are flop-count heuristics,
+ * src/layer2/bgreedy_contraction.jl).  The per-pair timings that train the
+ * model are measured by the backend itself. */
+
+/* Time `n_pairs` pairwise contractions with this context's kernels and
+ * storage policy (C = symdiff(A, B) as pq_contract_tensors).  Pair p has
+ * a_ranks[p] then b_ranks[p] consecutive entries in `labels` / `dims` (the
+ * extent of each label occurrence).  Each pair runs once to warm up, then
+ * `reps` times between CUDA events; ms[p] is the mean and feats[8p..8p+7] its
+ * shape features (as pq_plan_step_features). */
+int pq_measure_pairs(pq_ctx* ctx, int n_pairs, const int32_t* a_ranks, const int32_t* b_ranks,
+                     const int32_t* labels, const int64_t* dims, int reps, float* ms, double* feats);
+
+typedef struct pq_mlp pq_mlp;
+/* MLP n_in -> hidden (x hidden_layers, ReLU) -> 1, FP32 parameters in one
+ * flat buffer ordered W1 b1 W2 b2 ... (W_l row-major [in x out]), trained on
+ * the context's device by hand-written forward/backward/Adam kernels. */
+int pq_mlp_create(pq_ctx* ctx, int n_in, int hidden, int hidden_layers, uint64_t seed, pq_mlp** out);
+int pq_mlp_destroy(pq_mlp* m);
+int pq_mlp_num_params(pq_mlp* m, int64_t* n);
+int pq_mlp_get_params(pq_mlp* m, float* params, int64_t n);
+int pq_mlp_set_params(pq_mlp* m, const float* params, int64_t n);
+/* Mean-squared-error loss and its gradient w.r.t. all parameters for rows
+ * X[n x n_in] (row-major) with targets y[n]. */
+int pq_mlp_gradients(pq_mlp* m, const float* X, const float* y, int64_t n, float* grad, float* loss);
+/* Adam over `epochs` passes of shuffled mini-batches; the loss of the last
+ * batch is returned. */
+int pq_mlp_train(pq_mlp* m, const float* X, const float* y, int64_t n, int epochs, int batch, float lr,
+                 uint64_t seed, float* final_loss);
+/* Predictions for n rows; bf16 != 0 runs inference with bf16 weights and
+ * activations (FP32 accumulation). */
+int pq_mlp_predict(pq_mlp* m, const float* X, int64_t n, float* out, int bf16);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,15 @@ SIGNATURES = [
                                  C.c_int, C.c_uint64, i32p, f64p, i64p]),
     ("pq_plan_choose_slices", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_int, i32p,
                                         C.c_int, C.c_double, i32p, C.POINTER(C.c_int)]),
+    ("pq_measure_pairs", C.c_int, [vp, C.c_int, i32p, i32p, i32p, i64p, C.c_int, f32p, f64p]),
+    ("pq_mlp_create", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(vp)]),
+    ("pq_mlp_destroy", C.c_int, [vp]),
+    ("pq_mlp_num_params", C.c_int, [vp, i64p]),
+    ("pq_mlp_get_params", C.c_int, [vp, f32p, C.c_int64]),
+    ("pq_mlp_set_params", C.c_int, [vp, f32p, C.c_int64]),
+    ("pq_mlp_gradients", C.c_int, [vp, f32p, f32p, C.c_int64, f32p, f32p]),
+    ("pq_mlp_train", C.c_int, [vp, f32p, f32p, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, f32p]),
+    ("pq_mlp_predict", C.c_int, [vp, f32p, C.c_int64, f32p, C.c_int]),
 ]
 
 # exported by the library but optional for older builds

@@ -161,3 +161,24 @@ def test_reference_qasm_fixtures(O, name, n):
         ref = np.zeros(2**n)
         ref[0] = ref[-1] = 1 / math.sqrt(2)
         assert np.max(np.abs(np.abs(out) - ref)) < 1e-12
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    # pins the MLP oracle used to check the GPU training kernels
+    import mlp_oracle as MO
+
+    rng = np.random.default_rng(0)
+    n_in, hidden, layers = 5, 7, 3
+    npar = sum(a * b + b for a, b in MO.layer_shapes(n_in, hidden, layers))
+    p = rng.standard_normal(npar)
+    X = rng.standard_normal((11, n_in))
+    y = rng.standard_normal(11)
+    loss, g = MO.loss_and_grad(p, X, y, n_in, hidden, layers)
+    eps = 1e-6
+    for i in rng.choice(npar, 25, replace=False):
+        q = p.copy()
+        q[i] += eps
+        lp, _ = MO.loss_and_grad(q, X, y, n_in, hidden, layers)
+        q[i] -= 2 * eps
+        lm, _ = MO.loss_and_grad(q, X, y, n_in, hidden, layers)
+        assert abs((lp - lm) / (2 * eps) - g[i]) < 1e-6 * max(1.0, abs(g[i]))
