@@ -42,20 +42,38 @@ def random_pair_shapes(n, seed=0, max_log2=24, dim_choices=(2, 2, 2, 2, 3, 4, 8,
     (a_ranks, b_ranks, labels, dims) arrays of ``pq_measure_pairs``."""
     rng = np.random.default_rng(seed)
     a_ranks, b_ranks, labels, dims = [], [], [], []
-    for _ in range(n):
-        while True:
-            n_sh = int(rng.integers(0, 9))
-            n_a = int(rng.integers(0, 15))
-            n_b = int(rng.integers(0, 15))
-            if n_sh + n_a < 2 or n_sh + n_b < 1 or n_sh + n_a > 30 or n_sh + n_b > 30:
-                continue
-            d = [int(rng.choice(dim_choices)) for _ in range(n_sh + n_a + n_b)]
-            la = np.log2(d[:n_sh]).sum() + np.log2(d[n_sh:n_sh + n_a]).sum()
-            lb = np.log2(d[:n_sh]).sum() + np.log2(d[n_sh + n_a:]).sum()
-            lc = np.log2(d[n_sh:]).sum()
-            lk = np.log2(d[:n_sh]).sum()
-            if max(la, lb, lc) <= max_log2 and lc + lk <= max_cmacs_log2:
-                break
+    choices = [int(x) for x in dim_choices]
+    l2 = {x: float(np.log2(x)) for x in choices}
+    pool = [choices[i] for i in rng.integers(0, len(choices), 64 * n + 64)]
+    pi = [0]
+
+    def fill(budget, cap):
+        """Extents whose log2 sum stays within ``budget`` (at most ``cap`` modes)."""
+        out, s = [], 0.0
+        while len(out) < cap:
+            d = pool[pi[0]]
+            pi[0] += 1
+            if s + l2[d] > budget + 1e-9:
+                if s + 1.0 > budget + 1e-9:
+                    break
+                d = 2
+            out.append(d)
+            s += l2[d]
+        return out, s
+
+    u = rng.random((n, 3))
+    for i in range(n):
+        # log2 budgets: contracted, A-free, B-free, within every limit
+        lk = u[i, 0] * min(12.0, max_log2)
+        la = u[i, 1] * (max_log2 - lk)
+        lb = u[i, 2] * min(max_log2 - lk, max_log2 - la, max_cmacs_log2 - lk - la)
+        gk, sk = fill(lk, 8)
+        ga, sa = fill(la, 30 - len(gk))
+        gb, _ = fill(max(0.0, min(lb, max_cmacs_log2 - sk - sa)), 30 - len(gk))
+        if len(gk) + len(ga) < 1:
+            ga = [2]
+        d = gk + ga + gb
+        n_sh, n_a, n_b = len(gk), len(ga), len(gb)
         sh = list(range(n_sh))
         fa = list(range(n_sh, n_sh + n_a))
         fb = list(range(n_sh + n_a, n_sh + n_a + n_b))
@@ -71,15 +89,25 @@ def random_pair_shapes(n, seed=0, max_log2=24, dim_choices=(2, 2, 2, 2, 3, 4, 8,
             np.array(dims, np.int64))
 
 
-def measure_pairs(backend, shapes, reps=3, chunk=512):
-    """Time pairs on the GPU; returns (ms[n], feats[n, 8])."""
+def measure_pairs(backend, shapes, reps=3, chunk=512, budget_s=None, log=None):
+    """Time pairs on the GPU; returns (ms[n'], feats[n', 8]) for the first n'
+    pairs measured within ``budget_s`` seconds (all pairs if None)."""
+    import time
+
     a_r, b_r, lab, dims = shapes
     n = len(a_r)
     ms = np.empty(n, np.float32)
     feats = np.empty((n, 8), np.float64)
     lib = L.lib()
     pos = 0
+    t0 = time.perf_counter()
     for i0 in range(0, n, chunk):
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            if log:
+                log({"measured": i0, "seconds": time.perf_counter() - t0, "stopped": "time budget"})
+            return ms[:i0], feats[:i0]
+        if log and i0 % (chunk * 20) == 0:
+            log({"measured": i0, "seconds": time.perf_counter() - t0})
         i1 = min(n, i0 + chunk)
         cnt = int(a_r[i0:i1].sum() + b_r[i0:i1].sum())
         m = np.empty(i1 - i0, np.float32)
@@ -177,11 +205,16 @@ class CostModel:
         return m
 
 
-def train_cost_model(backend, n_pairs=200_000, seed=0, epochs=40, reps=3, log=None):
-    """Measure ``n_pairs`` random pairs on this GPU and train the model on them
-    (90/10 split).  Returns (model, stats)."""
-    shapes = random_pair_shapes(n_pairs, seed)
-    ms, feats = measure_pairs(backend, shapes, reps=reps)
+def train_cost_model(backend, n_pairs=200_000, seed=0, epochs=40, reps=3, log=None, budget_s=600.0,
+                     max_log2=22, max_cmacs_log2=27):
+    """Measure up to ``n_pairs`` random pairs on this GPU (within ``budget_s``
+    seconds) and train the model on them (90/10 split).  Returns (model, stats)."""
+    import time
+
+    shapes = random_pair_shapes(n_pairs, seed, max_log2=max_log2, max_cmacs_log2=max_cmacs_log2)
+    t0 = time.perf_counter()
+    ms, feats = measure_pairs(backend, shapes, reps=reps, budget_s=budget_s, log=log)
+    t_measure = time.perf_counter() - t0
     X = model_inputs(feats)
     y = np.log(np.maximum(ms.astype(np.float64), 1e-4) * 1e3).astype(np.float32)
     rng = np.random.default_rng(seed)
@@ -193,7 +226,8 @@ def train_cost_model(backend, n_pairs=200_000, seed=0, epochs=40, reps=3, log=No
     pred = model.predict(X[te], bf16=True)
     rmse = float(np.sqrt(np.mean((pred - y[te]) ** 2)))
     base = float(np.sqrt(np.mean((y[te] - y[tr].mean()) ** 2)))
-    stats = {"pairs": len(y), "train_loss": loss, "test_rmse_log": rmse, "test_rmse_mean_predictor": base,
+    stats = {"pairs": len(y), "measure_seconds": t_measure, "train_loss": loss, "test_rmse_log": rmse,
+             "test_rmse_mean_predictor": base,
              "median_abs_rel_err": float(np.median(np.abs(np.exp(pred - y[te]) - 1)))}
     if log:
         log(stats)

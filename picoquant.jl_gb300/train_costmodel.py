@@ -55,6 +55,7 @@ def main():
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--out", default=str(Path(__file__).resolve().parent / "costmodel_gb300.npz"))
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--budget", type=float, default=600.0, help="seconds allowed for measuring pairs")
     args = ap.parse_args()
     import __graft_entry__ as g
 
@@ -63,7 +64,8 @@ def main():
 
     be = pq.GB300Backend(pq.PREC_C64)
     t0 = time.perf_counter()
-    model, stats = CM.train_cost_model(be, n_pairs=args.pairs, seed=args.seed, epochs=args.epochs)
+    model, stats = CM.train_cost_model(be, n_pairs=args.pairs, seed=args.seed, epochs=args.epochs,
+                                       budget_s=args.budget, log=lambda d: print(json.dumps(d), flush=True))
     stats["seconds"] = time.perf_counter() - t0
     model.save(args.out, meta={"stats": json.dumps(stats)})
     print(json.dumps({"trained": stats}), flush=True)
