@@ -246,8 +246,8 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
     nodes, ranks, flat, dims, label_of = _leaf_arrays(network, out_edges)
     outl = [label_of[e] for e in out_edges]
     cands = []
-    s, c, m = sweep_steps(network, nodes, outl, label_of, ranks, flat, dims)
-    cands.append(("sweep", s))
+    for i, (s, c, m) in enumerate(sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, all_orders=True)):
+        cands.append((f"sweep{i}", s))
     if not out_edges or all(network.edges[e].src is not None for e in network.input_qubits):
         try:
             cands.append(("wavefunction", wavefunction_steps(network, nodes)))

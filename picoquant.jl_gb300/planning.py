@@ -349,13 +349,15 @@ def _node_qubit(network, node_label):
     return None
 
 
-def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None, flat=None, dims=None):
+def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None, flat=None, dims=None,
+                all_orders=False):
     """Qubit-sweep plan: contract each qubit's tensors along time into one
     tensor, then absorb qubits one at a time into a growing boundary.
 
-    Several qubit orders are tried (natural order, and greedy smallest-boundary
-    orders started from a few qubits); the cheapest by complex multiply-adds is
-    returned as (steps, cmacs, max_elems).
+    Several qubit orders are tried (natural and reversed order, and greedy
+    smallest-boundary orders started from a few qubits); the cheapest by
+    complex multiply-adds is returned as (steps, cmacs, max_elems), or every
+    order's triple when ``all_orders``.
     """
     leaves = leaves if leaves is not None else list(network.nodes.keys())
     groups: dict[int, list] = {}
@@ -432,11 +434,12 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
             labels |= ext[best]
         return order
 
-    orders = [list(qs)]
-    starts = [qs[0], qs[-1], qs[len(qs) // 2]]
+    orders = [list(qs), list(reversed(qs))]
+    nq = len(qs)
+    starts = [qs[0], qs[-1], qs[nq // 2], qs[nq // 4], qs[(3 * nq) // 4]]
     for s in dict.fromkeys(starts):
         orders.append(greedy_order(s))
-    best = None
+    found = []
     for order in orders:
         steps = list(base_steps)
         n2 = nxt
@@ -446,9 +449,10 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
             v = n2
             n2 += 1
         c, m = plan_cost(ranks, flat, dims, steps, out_labels)
-        if best is None or c < best[1]:
-            best = (steps, c, m)
-    return best
+        found.append((steps, c, m))
+    if all_orders:
+        return found
+    return min(found, key=lambda t: (t[1], t[2]))
 
 
 def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("sweep", "greedy", "wavefunction")):
