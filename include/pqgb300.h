@@ -131,6 +131,25 @@ int pq_view_tensor(pq_ctx* ctx, int64_t view_id, int64_t node, int bond_idx1,
  * written as `dtype` into host memory.  Synchronises. */
 int pq_gather_elements(pq_ctx* ctx, int64_t id, const int64_t* idx, int64_t n,
                        void* out, int dtype);
+/* pq_gather_elements for callers that cannot let the library allocate device
+ * memory (a host that owns and accounts every device allocation itself, such
+ * as a Julia process whose CUDA.jl pool must see all device memory, or an
+ * application running under a fixed device-memory budget).  No counterpart
+ * in the reference.  Same arguments, results and errors as
+ * pq_gather_elements, but the index list and the gathered values are staged
+ * in a fixed static device array instead of buffers allocated per call; the
+ * call allocates no device memory.
+ *   - At most 65536 indices per call; larger n fails with PQ_ERR_INVALID.
+ *   - The array (1.5 MiB) is reserved on every device that loads the
+ *     library until the process exits.
+ *   - The first call on a device looks the array's device address up; make
+ *     that first call before any stream capture on that device.
+ *   - All calls on a device share the array and each overwrites what the
+ *     previous one left (nothing in it needs to start zeroed); calls that
+ *     overlap on the GPU (other contexts' streams of the same device)
+ *     race on it. */
+int pq_gather_elements_noalloc(pq_ctx* ctx, int64_t id, const int64_t* idx, int64_t n,
+                               void* out, int dtype);
 
 /* ---- contraction plans ----------------------------------------------------
  * A plan is a whole pairwise contraction of a network, compiled once

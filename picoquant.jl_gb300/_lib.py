@@ -76,6 +76,7 @@ SIGNATURES = [
     ("pq_reshape_tensor", C.c_int, [vp, C.c_int64, C.c_int, i32p, i32p]),
     ("pq_view_tensor", C.c_int, [vp, C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64]),
     ("pq_gather_elements", C.c_int, [vp, C.c_int64, i64p, C.c_int64, vp, C.c_int]),
+    ("pq_gather_elements_noalloc", C.c_int, [vp, C.c_int64, i64p, C.c_int64, vp, C.c_int]),
     ("pq_plan_create", C.c_int, [vp, C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_int, i32p,
                                  C.POINTER(vp)]),
     ("pq_plan_destroy", C.c_int, [vp]),
