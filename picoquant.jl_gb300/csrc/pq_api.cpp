@@ -331,8 +331,8 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
       return st;
     }
     e = launch_tc(ctx->precision, A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, scratch, sbytes,
-                  ctx->stream);
-    ctx->launches += 4;
+                  ctx->d_status, ctx->stream);
+    ctx->launches += 3;
   } else if (pp.kclass == KC_GEMM) {
     e = launch_gemm(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
     ctx->launches += 1;

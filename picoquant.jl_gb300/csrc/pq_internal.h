@@ -140,7 +140,7 @@ cudaError_t launch_slice_sum(int dt, const void* X, int64_t n, int64_t nb,
 // Split-precision tensor-core GEMM-class contraction (pq_tc.cu).  Returns
 // cudaErrorNotSupported when the shape is not eligible.
 cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C,
-                      const GemmDesc& d, void* scratch, size_t scratch_bytes, cudaStream_t stream);
+                      const GemmDesc& d, void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream);
 size_t tc_scratch_bytes(int precision, const GemmDesc& d);
 bool tc_eligible(int precision, const GemmDesc& d);
 

@@ -60,8 +60,9 @@ int pq_measure_pairs(pq_ctx* c, int n_pairs, const int32_t* a_ranks, const int32
     cudaEventCreate(&e1);
     auto run = [&](int p) -> cudaError_t {
       const PairPlan& q = plans[p];
-      ctx->launches += q.kclass == KC_TC ? 4 : 1;
-      if (q.kclass == KC_TC) return launch_tc(ctx->precision, ta[p], tb[p], tc[p], A, B, C, q.m, S, smax, ctx->stream);
+      ctx->launches += q.kclass == KC_TC ? 3 : 1;
+      if (q.kclass == KC_TC)
+        return launch_tc(ctx->precision, ta[p], tb[p], tc[p], A, B, C, q.m, S, smax, ctx->d_status, ctx->stream);
       if (q.kclass == KC_GEMM) return launch_gemm(ta[p], tb[p], tc[p], A, B, C, q.m, ctx->stream);
       return launch_generic(ta[p], tb[p], tc[p], A, B, C, q.g, ctx->stream);
     };
