@@ -47,15 +47,23 @@ extern "C" {
 /* ---- context precision modes ------------------------------------------- *
  * PQ_PREC_C128   : tensors stored as complex128, all arithmetic FP64.
  *                  The plain complex-FP64 CUDA path.
- * PQ_PREC_C64    : tensors stored as complex64, FP32 arithmetic.
- * PQ_PREC_3XTF32 : complex64 storage; large contractions run as split
- *                  (hi+lo) TF32 tensor-core products with FP32 accumulation
- *                  (3 products per real GEMM, 3M complex trick).
- * PQ_PREC_3XBF16 : as 3XTF32 with bf16 hi/lo splits.                      */
+ * PQ_PREC_C64    : large tensors stored as complex64 (small ones, see
+ *                  pq_ctx_set_small_elems, as complex128); FP32 SIMT
+ *                  arithmetic with Kahan-compensated accumulation.
+ * PQ_PREC_3XTF32 : as PQ_PREC_C64, but large GEMM-shaped contractions run on
+ *                  the tcgen05 tensor cores: every real product split into
+ *                  TF32 hi+lo parts (3 products: hh, hl, lh), FP32 TMEM
+ *                  accumulation over 32-deep K chunks folded into
+ *                  Kahan-compensated FP32 sums.
+ * PQ_PREC_3XBF16 : accepted; runs as PQ_PREC_C64 (no bf16 tensor-core class:
+ *                  a bf16 hi/lo split cannot reach 1e-6 amplitude error).
+ * PQ_PREC_6XTF32 : as PQ_PREC_3XTF32 with a hi+mid+lo TF32 split and 6
+ *                  products (hh, hm, mh, hl, lh, mm) per real product.       */
 #define PQ_PREC_C128    0
 #define PQ_PREC_C64     1
 #define PQ_PREC_3XTF32  2
 #define PQ_PREC_3XBF16  3
+#define PQ_PREC_6XTF32  4
 
 #define PQ_MAX_RANK 56
 

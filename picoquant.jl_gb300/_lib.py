@@ -24,6 +24,7 @@ PREC_C128 = 0
 PREC_C64 = 1
 PREC_3XTF32 = 2
 PREC_3XBF16 = 3
+PREC_6XTF32 = 4
 
 PQ_MAX_RANK = 56
 

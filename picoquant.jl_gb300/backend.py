@@ -45,7 +45,8 @@ def record_memory_costs(backend, mem):
         backend.metrics.max_tensor_size = mem
 
 
-_PREC_NAMES = {L.PREC_C128: "c128", L.PREC_C64: "c64", L.PREC_3XTF32: "3xtf32", L.PREC_3XBF16: "3xbf16"}
+_PREC_NAMES = {L.PREC_C128: "c128", L.PREC_C64: "c64", L.PREC_3XTF32: "3xtf32", L.PREC_3XBF16: "3xbf16",
+               L.PREC_6XTF32: "6xtf32"}
 
 
 class GB300Backend:

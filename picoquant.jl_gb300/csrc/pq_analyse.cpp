@@ -237,7 +237,7 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
     if (!m.sa || !m.sb) k_both = false;
   bool gemm_shape = k_both && G.M >= 32 && G.N >= 32 && G.K >= 16 &&
                     (double)G.M * (double)G.N * (double)G.K * (double)G.Z >= double(1 << 20);
-  if (gemm_shape && (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_3XBF16) &&
+  if (gemm_shape && (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32) &&
       tc_eligible(precision, G))
     out.kclass = KC_TC;
   else if (gemm_shape || (k_both && out.ksize > kGenericKTab && G.M >= 8 && G.N >= 8))

@@ -1,31 +1,38 @@
 // Split-precision complex contraction on the 5th-generation tensor cores
-// (tcgen05, sm_103a): 3xTF32 products with FP32 accumulation in TMEM.
+// (tcgen05, sm_103a): TF32 split products, FP32 accumulation in TMEM over
+// short K chunks, chunk sums folded into Kahan-compensated FP32 registers.
 //
-//   C = A x B (complex), computed as three real accumulators per output tile
+//   C = A x B (complex), three real accumulators per output tile
 //     P1 = Ar.Br,  P2 = Ai.Bi,  P3 = Ar.Bi + Ai.Br     (Cr = P1 - P2, Ci = P3)
-//   with every real product split as  x.y ~ xh.yh + xh.yl + xl.yh
-//   where xh = tf32(x) and xl = tf32(x - xh) (round to nearest).
+//   Every real value is split into NS TF32 terms x = x0 + x1 (+ x2), each the
+//   round-to-nearest TF32 value of the remainder, and a real product is the
+//   sum of the term products with i + j < NS:
+//     NS = 2 (PQ_PREC_3XTF32): x0y0 + x0y1 + x1y0                (3 products)
+//     NS = 3 (PQ_PREC_6XTF32): x0y0 + x0y1 + x1y0 + x0y2 + x2y0 + x1y1  (6)
 //
-// Step 1 (k_tc_pack): each operand is gathered through its index map (any
-// mode order, batch modes) into four planes {re_hi, re_lo, im_hi, im_lo} of
-// FP32 values with TF32 precision, laid out tile by tile: a tile is 128 rows
-// (M or N) x 16 K values, stored in the canonical no-swizzle K-major UMMA
-// layout (8-row x 16-byte core matrices, 128 contiguous bytes each; core
-// matrices along K are 2048 bytes apart, along rows 128 bytes apart), so one
-// 8 KiB bulk copy moves one plane tile.  Rows and K past the operand are zero.
+// k_tc_pack gathers an operand through its index map (any mode order, batch
+// modes) into 2*NS planes {re terms, im terms} laid out tile by tile; a tile is
+// ROWS (128 for A, 64 for B) x 16 K values in the canonical no-swizzle
+// K-major UMMA layout: 8-row x 16-byte core matrices (128 contiguous bytes),
+// row-adjacent core matrices 128 bytes apart, K-adjacent ones ROWS*16 bytes
+// apart.  One bulk copy moves one plane tile.  Rows and K beyond the operand
+// are zero.
 //
-// Step 2 (k_tc_gemm): one CTA per 128 x 128 output tile (x batch), 6 warps:
-//   warp 0  producer: cp.async.bulk of 8 plane tiles per K step into a
-//           3-stage shared-memory ring (mbarrier complete_tx);
-//   warp 1  TMEM owner + MMA issuer: 24 tcgen05.mma (M=128, N=128, K=8) per
-//           16-deep K step into three 128-column FP32 accumulators, then
-//           tcgen05.commit to release the stage;
-//   warps 2-5 epilogue: tcgen05.ld of the accumulators (each warp its 32-lane
-//           quadrant), Cr = P1 - P2, Ci = P3, scattered to C through the
-//           result index map.
-// Every mbarrier wait is bounded; on expiry the kernel records an error in the
-// context's status word and runs to completion, so the host sees
-// PQ_ERR_DEVICE instead of a hang.
+// k_tc_gemm: one CTA per 128 x 64 output tile (x batch), 10 warps.
+//   warp 0   producer: cp.async.bulk of the 4*NS plane tiles of one K step
+//            into a shared-memory ring (mbarrier complete_tx);
+//   warp 1   allocates TMEM and issues tcgen05.mma (M=128, N=64, K=8); the K
+//            loop is cut into 32-deep chunks, alternating between two sets of
+//            three 64-column FP32 accumulators, each set committed to the
+//            epilogue when its chunk is done;
+//   warps 2-9 epilogue: warp w reads TMEM lanes 32*(w%4).. and 32 of the 64
+//            columns, folds each chunk's (P1 - P2, P3) into Kahan sums, hands
+//            the accumulator set back, and finally scatters C through the
+//            result index map.
+// Accumulating only 32 K values inside the tensor core keeps its FP32 adder
+// error from growing with K.  Every mbarrier wait is bounded; on expiry the
+// kernel records an error in the context's status word and runs to the end
+// (TMEM is always released), so the host sees PQ_ERR_DEVICE, not a hang.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -36,16 +43,22 @@ namespace pq {
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 16;      // tile extents
-constexpr int kStages = 3;
-constexpr int kPlanes = 4;                       // re_hi, re_lo, im_hi, im_lo
-constexpr int kTileFloats = TM * TK;             // 2048 floats = 8 KiB per plane tile
-constexpr uint32_t kTileBytes = kTileFloats * 4;
-constexpr uint32_t kStageBytes = 2 * kPlanes * kTileBytes;  // A and B planes
-constexpr int kThreads = 192;
-constexpr uint32_t kTmemCols = 512;              // three 128-column accumulators
-constexpr uint32_t kWaitLimit = 1u << 22;        // mbarrier polls before giving up
+constexpr int TM = 128, TN = 64, TK = 16;
+constexpr int kChunkTiles = 2;                 // K tiles per TMEM chunk (32 K values)
+constexpr int kThreads = 320;
+constexpr uint32_t kTmemCols = 512;            // 2 sets x 3 accumulators x 64 columns = 384 used
+constexpr uint32_t kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 constexpr int kStatusTcTimeout = 0x7c01;
+constexpr int kATile = TM * TK;                // floats per A plane tile (8 KiB)
+constexpr int kBTile = TN * TK;                // floats per B plane tile (4 KiB)
+
+template <int NS>
+struct Cfg {
+  static constexpr int planes = 2 * NS;                                  // per operand
+  static constexpr uint32_t stage_bytes = planes * (kATile + kBTile) * 4;
+  static constexpr int stages = NS == 2 ? 4 : 3;
+  static constexpr int products = NS == 2 ? 3 : 6;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -55,18 +68,20 @@ __device__ __forceinline__ float tf32_rna(float x) {
   return __uint_as_float(r);
 }
 
-// hi/lo TF32 split of a real value held in FP32 or FP64.
-__device__ __forceinline__ void split(float x, float& hi, float& lo) {
-  hi = tf32_rna(x);
-  lo = tf32_rna(x - hi);
+template <int NS>
+__device__ __forceinline__ void split(float x, float* t) {
+  t[0] = tf32_rna(x);
+  float r = x - t[0];
+  t[1] = tf32_rna(r);
+  if (NS == 3) t[2] = tf32_rna(r - t[1]);
 }
-__device__ __forceinline__ void split(double x, float& hi, float& lo) {
-  hi = tf32_rna((float)x);
-  lo = tf32_rna((float)(x - (double)hi));
+template <int NS>
+__device__ __forceinline__ void split(double x, float* t) {
+  t[0] = tf32_rna((float)x);
+  double r = x - (double)t[0];
+  t[1] = tf32_rna((float)r);
+  if (NS == 3) t[2] = tf32_rna((float)(r - (double)t[1]));
 }
-
-// Offset (in floats) of element (row r, k) inside one plane tile.
-__device__ __forceinline__ int tile_off(int r, int k) { return ((k >> 2) * 16 + (r >> 3)) * 32 + (r & 7) * 4 + (k & 3); }
 
 __device__ __forceinline__ int64_t decode(int64_t x, int n, const int64_t* dim, const int64_t* s1) {
   int64_t o = 0;
@@ -79,47 +94,49 @@ __device__ __forceinline__ int64_t decode(int64_t x, int n, const int64_t* dim, 
   return o;
 }
 
-// Pack operand X (side 0: A with m modes, side 1: B with n modes) into planes.
-// planes layout: [z][row tile][k tile][plane][2048 floats].
-template <typename T>
+// Pack operand X (side 0: A with m modes, side 1: B with n modes) into planes
+// laid out [z][row tile][k tile][plane][ROWS*16 floats].
+template <typename T, int NS, int ROWS>
 __global__ void __launch_bounds__(256) k_tc_pack(const T* __restrict__ X, float* __restrict__ planes,
                                                  const __grid_constant__ GemmDesc d, int side, int64_t rows,
                                                  int64_t rtiles, int64_t ktiles) {
-  __shared__ int64_t roff[TM];
+  constexpr int TILE = ROWS * TK, GROUPS = ROWS / 8;
+  __shared__ int64_t roff[ROWS];
   __shared__ int64_t koff[TK];
-  const int64_t kt = blockIdx.x, rt = blockIdx.y;
-  const int64_t z = blockIdx.z;
+  const int64_t kt = blockIdx.x, rt = blockIdx.y, z = blockIdx.z;
   const int nrm = side == 0 ? d.nm : d.nn;
   const int64_t* rdim = side == 0 ? d.mdim : d.ndim;
   const int64_t* rstr = side == 0 ? d.msa : d.nsb;
   const int64_t* kstr = side == 0 ? d.ksa : d.ksb;
   const int64_t* zstr = side == 0 ? d.zsa : d.zsb;
-  const int t = threadIdx.x;
-  if (t < TM) {
-    int64_t r = rt * TM + t;
-    roff[t] = r < rows ? decode(r, nrm, rdim, rstr) : -1;
-  } else if (t < TM + TK) {
-    int64_t k = kt * TK + (t - TM);
-    koff[t - TM] = k < d.K ? decode(k, d.nk, d.kdim, kstr) : -1;
+  for (int t = threadIdx.x; t < ROWS + TK; t += blockDim.x) {
+    if (t < ROWS) {
+      int64_t r = rt * ROWS + t;
+      roff[t] = r < rows ? decode(r, nrm, rdim, rstr) : -1;
+    } else {
+      int64_t k = kt * TK + (t - ROWS);
+      koff[t - ROWS] = k < d.K ? decode(k, d.nk, d.kdim, kstr) : -1;
+    }
   }
   __syncthreads();
   const int64_t zo = decode(z, d.nz, d.zdim, zstr);
-  float* tile = planes + (((z * rtiles + rt) * ktiles + kt) * kPlanes) * (int64_t)kTileFloats;
-  for (int o = t; o < kTileFloats; o += blockDim.x) {
-    // invert tile_off: o = ((kc*16 + g)*32) + r8*4 + k4
+  float* tile = planes + (((z * rtiles + rt) * ktiles + kt) * (2 * NS)) * (int64_t)TILE;
+  for (int o = threadIdx.x; o < TILE; o += blockDim.x) {
+    // o = ((kc * GROUPS + g) * 32) + r8 * 4 + k4
     const int core = o >> 5, within = o & 31;
-    const int kc = core >> 4, g = core & 15;
+    const int kc = core / GROUPS, g = core - kc * GROUPS;
     const int r = g * 8 + (within >> 2), k = kc * 4 + (within & 3);
-    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    float re[3] = {0.f, 0.f, 0.f}, im[3] = {0.f, 0.f, 0.f};
     if (roff[r] >= 0 && koff[k] >= 0) {
       T v = X[zo + roff[r] + koff[k]];
-      split(v.x, rh, rl);
-      split(v.y, ih, il);
+      split<NS>(v.x, re);
+      split<NS>(v.y, im);
     }
-    tile[0 * kTileFloats + o] = rh;
-    tile[1 * kTileFloats + o] = rl;
-    tile[2 * kTileFloats + o] = ih;
-    tile[3 * kTileFloats + o] = il;
+#pragma unroll
+    for (int t = 0; t < NS; ++t) {
+      tile[(0 * NS + t) * TILE + o] = re[t];
+      tile[(1 * NS + t) * TILE + o] = im[t];
+    }
   }
 }
 
@@ -129,6 +146,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   for (uint32_t i = 0; i < kWaitLimit; ++i) {
@@ -159,11 +179,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 }
 // Instruction descriptor for kind::tf32, FP32 accumulation, both K-major.
 __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
-  return (1u << 4)                        // D: F32
-         | (2u << 7)                      // A: TF32
-         | (2u << 10)                     // B: TF32
-         | ((uint32_t)(n >> 3) << 17)     // N / 8
-         | ((uint32_t)(m >> 4) << 24);    // M / 16
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
@@ -176,59 +192,64 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+template <int NS>
 struct alignas(1024) TcSmem {
-  float stage[kStages][2 * kPlanes][kTileFloats];  // A planes then B planes
-  uint64_t full[kStages];
-  uint64_t empty[kStages];
-  uint64_t accum;
+  float stage[Cfg<NS>::stages][Cfg<NS>::planes * (kATile + kBTile)];  // A planes, then B planes
+  uint64_t full[Cfg<NS>::stages];
+  uint64_t empty[Cfg<NS>::stages];
+  uint64_t accf[2];
+  uint64_t acce[2];
   uint32_t tmem_base;
   int64_t cm[TM];
   int64_t cn[TN];
 };
 
-template <typename TC>
+template <typename TC, int NS>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const float* __restrict__ pa, const float* __restrict__ pb, TC* __restrict__ C,
               const __grid_constant__ GemmDesc d, int64_t mtiles, int64_t ntiles, int64_t ktiles, int* status) {
+  using CF = Cfg<NS>;
+  constexpr int S = CF::stages, P = CF::planes;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
+  TcSmem<NS>& sm = *reinterpret_cast<TcSmem<NS>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nt = blockIdx.x, mt = blockIdx.y, z = blockIdx.z;
+  const int64_t nchunks = (ktiles + kChunkTiles - 1) / kChunkTiles;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&S.full[s], 1);
-      mbar_init(&S.empty[s], 1);
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
     }
-    mbar_init(&S.accum, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accf[b], 1);
+      mbar_init(&sm.acce[b], 8);  // one arrival per epilogue warp
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // result offsets of this tile's rows / columns
   for (int i = threadIdx.x; i < TM + TN; i += blockDim.x) {
     if (i < TM) {
       int64_t m = mt * TM + i;
-      S.cm[i] = m < d.M ? decode(m, d.nm, d.mdim, d.msc) : -1;
+      sm.cm[i] = m < d.M ? decode(m, d.nm, d.mdim, d.msc) : -1;
     } else {
       int64_t n = nt * TN + (i - TM);
-      S.cn[i - TM] = n < d.N ? decode(n, d.nn, d.ndim, d.nsc) : -1;
+      sm.cn[i - TM] = n < d.N ? decode(n, d.nn, d.ndim, d.nsc) : -1;
     }
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_base)),
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
                  "r"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -236,100 +257,122 @@ __global__ void __launch_bounds__(kThreads, 1)
   fence_before();
   __syncthreads();
   fence_after();
-  const uint32_t tmem = S.tmem_base;
+  const uint32_t tmem = sm.tmem_base;
   bool ok = true;
 
-  const float* atile = pa + ((z * mtiles + mt) * ktiles) * (int64_t)(kPlanes * kTileFloats);
-  const float* btile = pb + ((z * ntiles + nt) * ktiles) * (int64_t)(kPlanes * kTileFloats);
+  const float* atile = pa + ((z * mtiles + mt) * ktiles) * (int64_t)(P * kATile);
+  const float* btile = pb + ((z * ntiles + nt) * ktiles) * (int64_t)(P * kBTile);
 
   if (warp == 0) {
     if (lane == 0) {
-      for (int64_t kt = 0; kt < ktiles && ok; ++kt) {
-        const int s = (int)(kt % kStages);
-        const uint32_t ph = (uint32_t)((kt / kStages) & 1);
-        if (!mbar_wait(&S.empty[s], ph ^ 1)) {
+      for (int64_t kt = 0; kt < ktiles; ++kt) {
+        const int s = (int)(kt % S);
+        const uint32_t ph = (uint32_t)((kt / S) & 1);
+        if (!mbar_wait(&sm.empty[s], ph ^ 1)) {
           ok = false;
           break;
         }
-        mbar_expect_tx(&S.full[s], kStageBytes);
-        const float* a = atile + kt * (kPlanes * kTileFloats);
-        const float* b = btile + kt * (kPlanes * kTileFloats);
+        mbar_expect_tx(&sm.full[s], CF::stage_bytes);
+        const float* a = atile + kt * (P * kATile);
+        const float* b = btile + kt * (P * kBTile);
+        float* dst = sm.stage[s];
 #pragma unroll
-        for (int p = 0; p < kPlanes; ++p) {
-          bulk_g2s(S.stage[s][p], a + p * kTileFloats, kTileBytes, &S.full[s]);
-          bulk_g2s(S.stage[s][kPlanes + p], b + p * kTileFloats, kTileBytes, &S.full[s]);
+        for (int p = 0; p < P; ++p) {
+          bulk_g2s(dst + p * kATile, a + p * kATile, kATile * 4, &sm.full[s]);
+          bulk_g2s(dst + P * kATile + p * kBTile, b + p * kBTile, kBTile * 4, &sm.full[s]);
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(TM, TN);
-      constexpr uint32_t LBO = 2048, SBO = 128;  // K-direction / row-direction core matrix strides
-      const uint32_t d1 = tmem, d2 = tmem + 128, d3 = tmem + 256;
-      for (int64_t kt = 0; kt < ktiles && ok; ++kt) {
-        const int s = (int)(kt % kStages);
-        const uint32_t ph = (uint32_t)((kt / kStages) & 1);
-        if (!mbar_wait(&S.full[s], ph)) {
+      constexpr uint32_t ALBO = (TM / 8) * 128, BLBO = (TN / 8) * 128, SBO = 128;
+      int64_t kt = 0;
+      for (int64_t c = 0; c < nchunks && ok; ++c) {
+        const int b = (int)(c & 1);
+        const uint32_t use = (uint32_t)((c >> 1) & 1);
+        if (!mbar_wait(&sm.acce[b], use ^ 1)) {
           ok = false;
           break;
         }
         fence_after();
+        const uint32_t d1 = tmem + (uint32_t)b * 192, d2 = d1 + 64, d3 = d1 + 128;
+        for (int t = 0; t < kChunkTiles && kt < ktiles; ++t, ++kt) {
+          const int s = (int)(kt % S);
+          const uint32_t ph = (uint32_t)((kt / S) & 1);
+          if (!mbar_wait(&sm.full[s], ph)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t sa = smem_u32(sm.stage[s]);
+          const uint32_t sb = sa + P * kATile * 4;
 #pragma unroll
-        for (int j = 0; j < TK / 8; ++j) {
-          const uint32_t off = (uint32_t)j * 2 * LBO;
-          const uint64_t arh = smem_desc(smem_u32(S.stage[s][0]) + off, LBO, SBO);
-          const uint64_t arl = smem_desc(smem_u32(S.stage[s][1]) + off, LBO, SBO);
-          const uint64_t aih = smem_desc(smem_u32(S.stage[s][2]) + off, LBO, SBO);
-          const uint64_t ail = smem_desc(smem_u32(S.stage[s][3]) + off, LBO, SBO);
-          const uint64_t brh = smem_desc(smem_u32(S.stage[s][4]) + off, LBO, SBO);
-          const uint64_t brl = smem_desc(smem_u32(S.stage[s][5]) + off, LBO, SBO);
-          const uint64_t bih = smem_desc(smem_u32(S.stage[s][6]) + off, LBO, SBO);
-          const uint64_t bil = smem_desc(smem_u32(S.stage[s][7]) + off, LBO, SBO);
-          const uint32_t acc = (kt > 0 || j > 0) ? 1u : 0u;
-          // P1 = Ar.Br
-          mma_tf32(d1, arh, brh, idesc, acc);
-          mma_tf32(d1, arh, brl, idesc, 1u);
-          mma_tf32(d1, arl, brh, idesc, 1u);
-          // P2 = Ai.Bi
-          mma_tf32(d2, aih, bih, idesc, acc);
-          mma_tf32(d2, aih, bil, idesc, 1u);
-          mma_tf32(d2, ail, bih, idesc, 1u);
-          // P3 = Ar.Bi + Ai.Br
-          mma_tf32(d3, arh, bih, idesc, acc);
-          mma_tf32(d3, arh, bil, idesc, 1u);
-          mma_tf32(d3, arl, bih, idesc, 1u);
-          mma_tf32(d3, aih, brh, idesc, 1u);
-          mma_tf32(d3, aih, brl, idesc, 1u);
-          mma_tf32(d3, ail, brh, idesc, 1u);
+          for (int j = 0; j < TK / 8; ++j) {
+            const uint32_t oa = (uint32_t)j * 2 * ALBO, ob = (uint32_t)j * 2 * BLBO;
+            uint32_t acc = (t == 0 && j == 0) ? 0u : 1u;
+#pragma unroll
+            for (int q = 0; q < CF::products; ++q) {
+              // term pairs (i, j) with i + j < NS: (0,0) (0,1) (1,0) (0,2) (2,0) (1,1)
+              const int ti = (q == 2) ? 1 : (q == 4) ? 2 : (q == 5) ? 1 : 0;
+              const int tj = (q == 1) ? 1 : (q == 3) ? 2 : (q == 5) ? 1 : 0;
+              const uint64_t ar = smem_desc(sa + (0 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
+              const uint64_t ai = smem_desc(sa + (1 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
+              const uint64_t br = smem_desc(sb + (0 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
+              const uint64_t bi = smem_desc(sb + (1 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
+              mma_tf32(d1, ar, br, idesc, acc);
+              mma_tf32(d2, ai, bi, idesc, acc);
+              mma_tf32(d3, ar, bi, idesc, acc);
+              mma_tf32(d3, ai, br, idesc, 1u);
+              acc = 1u;
+            }
+          }
+          mma_commit(&sm.empty[s]);  // smem stage free once these MMAs finish
         }
-        mma_commit(&S.empty[s]);  // stage reusable once these MMAs finish
+        mma_commit(&sm.accf[b]);  // chunk accumulators ready for the epilogue
       }
-      mma_commit(&S.accum);  // accumulators complete
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quadrant = warp % 4
-    const int q = warp & 3;
+    // epilogue: warp w reads TMEM lanes of quadrant w % 4, columns [32h, 32h+32)
+    const int q = warp & 3, h = (warp - 2) >> 2;
     const int row = q * 32 + lane;
-    if (!mbar_wait(&S.accum, 0)) ok = false;
-    ok = __all_sync(0xffffffffu, ok);  // the TMEM loads below are warp-collective
-    fence_after();
-    if (ok) {
-      const int64_t cmr = S.cm[row];
-      const int64_t zc = decode(z, d.nz, d.zdim, d.zsc);
-      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-#pragma unroll 1
-      for (int c0 = 0; c0 < TN; c0 += 16) {
-        float p1[16], p2[16], p3[16];
-        tmem_ld16(lane_base + c0, p1);
-        tmem_ld16(lane_base + 128 + c0, p2);
-        tmem_ld16(lane_base + 256 + c0, p3);
-        tmem_wait_ld();
-        if (cmr >= 0) {
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    KahanC acc[32];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int64_t cnj = S.cn[c0 + j];
-            if (cnj >= 0) C[zc + cmr + cnj] = store_as<TC>(make_float2(p1[j] - p2[j], p3[j]));
-          }
+    for (int j = 0; j < 32; ++j) kahan_init(acc[j]);
+    for (int64_t c = 0; c < nchunks; ++c) {
+      const int b = (int)(c & 1);
+      const uint32_t use = (uint32_t)((c >> 1) & 1);
+      bool got = mbar_wait(&sm.accf[b], use);
+      got = __all_sync(0xffffffffu, got);  // the TMEM loads below are warp-collective
+      if (!got) {
+        ok = false;
+        break;
+      }
+      fence_after();
+#pragma unroll
+      for (int piece = 0; piece < 4; ++piece) {
+        const uint32_t col = (uint32_t)(b * 192 + h * 32 + piece * 8);
+        float p1[8], p2[8], p3[8];
+        tmem_ld8(lane_base + col, p1);
+        tmem_ld8(lane_base + col + 64, p2);
+        tmem_ld8(lane_base + col + 128, p3);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) kahan_add(acc[piece * 8 + j], make_float2(p1[j] - p2[j], p3[j]));
+      }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acce[b]);
+    }
+    if (ok) {
+      const int64_t cmr = sm.cm[row];
+      const int64_t zc = decode(z, d.nz, d.zdim, d.zsc);
+      if (cmr >= 0) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int64_t cnj = sm.cn[h * 32 + j];
+          if (cnj >= 0) C[zc + cmr + cnj] = store_as<TC>(kahan_value(acc[j]));
         }
       }
     }
@@ -345,64 +388,75 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+int splits_of(int precision) { return precision == PQ_PREC_6XTF32 ? 3 : 2; }
+
+template <typename T, int NS>
+void pack_both(const void* A, int ta, const void* B, int tb, float* pa, float* pb, const GemmDesc& d, int64_t mt,
+               int64_t nt, int64_t kt, cudaStream_t s) {
+  dim3 ga((unsigned)kt, (unsigned)mt, (unsigned)d.Z), gb((unsigned)kt, (unsigned)nt, (unsigned)d.Z);
+  (void)sizeof(T);
+  if (ta == PQ_C128)
+    k_tc_pack<double2, NS, TM><<<ga, 256, 0, s>>>((const double2*)A, pa, d, 0, d.M, mt, kt);
+  else
+    k_tc_pack<float2, NS, TM><<<ga, 256, 0, s>>>((const float2*)A, pa, d, 0, d.M, mt, kt);
+  if (tb == PQ_C128)
+    k_tc_pack<double2, NS, TN><<<gb, 256, 0, s>>>((const double2*)B, pb, d, 1, d.N, nt, kt);
+  else
+    k_tc_pack<float2, NS, TN><<<gb, 256, 0, s>>>((const float2*)B, pb, d, 1, d.N, nt, kt);
+}
+
+template <typename TC, int NS>
+cudaError_t gemm_launch(const float* pa, const float* pb, void* C, const GemmDesc& d, int64_t mt, int64_t nt,
+                        int64_t kt, int* status, cudaStream_t s) {
+  static_assert(sizeof(TcSmem<NS>) + 1024 <= 232448, "shared memory layout exceeds 227 KiB");
+  // the whole opt-in shared memory (one CTA per SM either way): the ring plus
+  // slack past the last stage
+  const size_t smem = 232448;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<TC, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)d.Z);
+  k_tc_gemm<TC, NS><<<grid, kThreads, smem, s>>>(pa, pb, (TC*)C, d, mt, nt, kt, status);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 bool tc_eligible(int precision, const GemmDesc& d) {
-  if (precision != PQ_PREC_3XTF32) return false;
+  if (precision != PQ_PREC_3XTF32 && precision != PQ_PREC_6XTF32) return false;
   if (d.M < 64 || d.N < 64 || d.K < 16) return false;
   if (d.Z > 65535 || ceil_div(d.N, TN) > 2147483647LL || ceil_div(d.M, TM) > 65535) return false;
-  // packed planes (16 bytes per complex element of A and B) stay below 24 GiB
   return tc_scratch_bytes(precision, d) <= (size_t(24) << 30);
 }
 
 size_t tc_scratch_bytes(int precision, const GemmDesc& d) {
-  (void)precision;
+  const int P = 2 * splits_of(precision);
   const int64_t mt = ceil_div(d.M, TM), nt = ceil_div(d.N, TN), kt = ceil_div(d.K, TK);
-  const int64_t per_tile = (int64_t)kPlanes * kTileFloats * 4;
-  return (size_t)(d.Z * (mt + nt) * kt * per_tile) + 1024;
+  return (size_t)(d.Z * (mt * kATile + nt * kBTile) * kt * P * 4) + 1024;
 }
 
 cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
                       void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream) {
   if (!tc_eligible(precision, d)) return cudaErrorNotSupported;
   if (!scratch || scratch_bytes < tc_scratch_bytes(precision, d)) return cudaErrorInvalidValue;
+  const int NS = splits_of(precision);
   const int64_t mt = ceil_div(d.M, TM), nt = ceil_div(d.N, TN), kt = ceil_div(d.K, TK);
   float* pa = (float*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
-  float* pb = pa + d.Z * mt * kt * (int64_t)(kPlanes * kTileFloats);
-  dim3 ga((unsigned)kt, (unsigned)mt, (unsigned)d.Z), gb((unsigned)kt, (unsigned)nt, (unsigned)d.Z);
-  if (ta == PQ_C128)
-    k_tc_pack<double2><<<ga, 256, 0, stream>>>((const double2*)A, pa, d, 0, d.M, mt, kt);
-  else
-    k_tc_pack<float2><<<ga, 256, 0, stream>>>((const float2*)A, pa, d, 0, d.M, mt, kt);
-  if (tb == PQ_C128)
-    k_tc_pack<double2><<<gb, 256, 0, stream>>>((const double2*)B, pb, d, 1, d.N, nt, kt);
-  else
-    k_tc_pack<float2><<<gb, 256, 0, stream>>>((const float2*)B, pb, d, 1, d.N, nt, kt);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  // the whole opt-in shared memory (one CTA per SM either way): the ring plus
-  // slack past the last stage
-  static_assert(sizeof(TcSmem) + 1024 <= 232448, "shared memory layout exceeds 227 KiB");
-  const size_t smem = 232448;
-  dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)d.Z);
-  if (tc == PQ_C128) {
-    static bool attr = false;
-    if (!attr) {
-      e = cudaFuncSetAttribute(k_tc_gemm<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
-    k_tc_gemm<double2><<<grid, kThreads, smem, stream>>>(pa, pb, (double2*)C, d, mt, nt, kt, status);
-  } else {
-    static bool attr = false;
-    if (!attr) {
-      e = cudaFuncSetAttribute(k_tc_gemm<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
-    k_tc_gemm<float2><<<grid, kThreads, smem, stream>>>(pa, pb, (float2*)C, d, mt, nt, kt, status);
+  float* pb = pa + d.Z * mt * kt * (int64_t)(2 * NS * kATile);
+  cudaError_t e;
+  if (NS == 2) {
+    pack_both<float, 2>(A, ta, B, tb, pa, pb, d, mt, nt, kt, stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return tc == PQ_C128 ? gemm_launch<double2, 2>(pa, pb, C, d, mt, nt, kt, status, stream)
+                         : gemm_launch<float2, 2>(pa, pb, C, d, mt, nt, kt, status, stream);
   }
-  return cudaGetLastError();
+  pack_both<float, 3>(A, ta, B, tb, pa, pb, d, mt, nt, kt, stream);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return tc == PQ_C128 ? gemm_launch<double2, 3>(pa, pb, C, d, mt, nt, kt, status, stream)
+                       : gemm_launch<float2, 3>(pa, pb, C, d, mt, nt, kt, status, stream);
 }
 
 }  // namespace pq
