@@ -53,7 +53,7 @@ extern "C" {
  * PQ_PREC_3XTF32 : as PQ_PREC_C64, but large GEMM-shaped contractions run on
  *                  the tcgen05 tensor cores: every real product split into
  *                  TF32 hi+lo parts (3 products: hh, hl, lh), FP32 TMEM
- *                  accumulation over 32-deep K chunks folded into
+ *                  accumulation over 8-deep K chunks folded into
  *                  Kahan-compensated FP32 sums.
  * PQ_PREC_3XBF16 : accepted; runs as PQ_PREC_C64 (no bf16 tensor-core class:
  *                  a bf16 hi/lo split cannot reach 1e-6 amplitude error).

@@ -235,7 +235,9 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
   bool k_both = true;
   for (const Mode& m : gk)
     if (!m.sa || !m.sb) k_both = false;
-  bool gemm_shape = k_both && G.M >= 32 && G.N >= 32 && G.K >= 16 &&
+  // square tiles for M, N >= 32; the narrow tiles take one side down to 8
+  const bool narrow = std::min(G.M, G.N) >= 8 && std::max(G.M, G.N) >= 256;
+  bool gemm_shape = k_both && G.K >= 16 && ((G.M >= 32 && G.N >= 32) || narrow) &&
                     (double)G.M * (double)G.N * (double)G.K * (double)G.Z >= double(1 << 20);
   if (gemm_shape && (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32) &&
       tc_eligible(precision, G))

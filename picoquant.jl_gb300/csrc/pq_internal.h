@@ -48,6 +48,10 @@ struct GemmDesc {
 };
 
 enum KernelClass : int { KC_GENERIC = 0, KC_GEMM = 1, KC_TC = 2, KC_COPY = 3 };
+// SIMT GEMM tile shapes: 64x64, 256x16 (narrow N), 16x256 (narrow M).
+enum GemmShape : int { GEMM_SQUARE = 0, GEMM_TALL = 1, GEMM_WIDE = 2 };
+struct GemmDesc;
+int gemm_tile_shape(const GemmDesc& d);
 
 // Host-side analysis of one contraction.
 struct PairPlan {

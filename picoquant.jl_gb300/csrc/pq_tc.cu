@@ -2,8 +2,8 @@
 // (tcgen05, sm_103a): TF32 split products, FP32 accumulation in TMEM over
 // short K chunks, chunk sums folded into Kahan-compensated FP32 registers.
 //
-//   C = A x B (complex), three real accumulators per output tile
-//     P1 = Ar.Br,  P2 = Ai.Bi,  P3 = Ar.Bi + Ai.Br     (Cr = P1 - P2, Ci = P3)
+//   C = A x B (complex), four real accumulators per output tile
+//     P1 = Ar.Br,  P2 = Ai.Bi,  P3 = Ar.Bi,  P4 = Ai.Br  (Cr = P1 - P2, Ci = P3 + P4)
 //   Every real value is split into NS TF32 terms x = x0 + x1 (+ x2), each the
 //   round-to-nearest TF32 value of the remainder, and a real product is the
 //   sum of the term products with i + j < NS:
@@ -21,16 +21,16 @@
 // k_tc_gemm: one CTA per 128 x 64 output tile (x batch), 10 warps.
 //   warp 0   producer: cp.async.bulk of the 4*NS plane tiles of one K step
 //            into a shared-memory ring (mbarrier complete_tx);
-//   warp 1   allocates TMEM and issues tcgen05.mma (M=128, N=64, K=8); the K
-//            loop is cut into 32-deep chunks, alternating between two sets of
-//            three 64-column FP32 accumulators, each set committed to the
-//            epilogue when its chunk is done;
+//   warp 1   allocates TMEM and issues tcgen05.mma (M=128, N=64, K=8); every
+//            8-deep K step is one chunk, alternating between two sets of four
+//            64-column FP32 accumulators, committed to the epilogue per chunk;
 //   warps 2-9 epilogue: warp w reads TMEM lanes 32*(w%4).. and 32 of the 64
-//            columns, folds each chunk's (P1 - P2, P3) into Kahan sums, hands
-//            the accumulator set back, and finally scatters C through the
-//            result index map.
-// Accumulating only 32 K values inside the tensor core keeps its FP32 adder
-// error from growing with K.  Every mbarrier wait is bounded; on expiry the
+//            columns, folds each chunk's (P1 - P2, P3 + P4) into Kahan sums,
+//            hands the accumulator set back, and finally scatters C through
+//            the result index map.
+// The tensor core rounds accumulations toward zero; each chunk takes one such
+// rounding at full magnitude (its hi x hi product is issued last) and chunks
+// are summed with compensation, which keeps the bias from growing with K.  Every mbarrier wait is bounded; on expiry the
 // kernel records an error in the context's status word and runs to the end
 // (TMEM is always released), so the host sees PQ_ERR_DEVICE, not a hang.
 #include <cuda_runtime.h>
@@ -44,9 +44,8 @@ namespace pq {
 namespace {
 
 constexpr int TM = 128, TN = 64, TK = 16;
-constexpr int kChunkTiles = 2;                 // K tiles per TMEM chunk (32 K values)
 constexpr int kThreads = 320;
-constexpr uint32_t kTmemCols = 512;            // 2 sets x 3 accumulators x 64 columns = 384 used
+constexpr uint32_t kTmemCols = 512;            // 2 sets x 4 accumulators x 64 columns
 constexpr uint32_t kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 constexpr int kStatusTcTimeout = 0x7c01;
 constexpr int kATile = TM * TK;                // floats per A plane tile (8 KiB)
@@ -226,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   TcSmem<NS>& sm = *reinterpret_cast<TcSmem<NS>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nt = blockIdx.x, mt = blockIdx.y, z = blockIdx.z;
-  const int64_t nchunks = (ktiles + kChunkTiles - 1) / kChunkTiles;
+  const int64_t nchunks = ktiles * (TK / 8);  // one chunk per 8-deep K step
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -287,49 +286,51 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(TM, TN);
       constexpr uint32_t ALBO = (TM / 8) * 128, BLBO = (TN / 8) * 128, SBO = 128;
-      int64_t kt = 0;
-      for (int64_t c = 0; c < nchunks && ok; ++c) {
-        const int b = (int)(c & 1);
-        const uint32_t use = (uint32_t)((c >> 1) & 1);
-        if (!mbar_wait(&sm.acce[b], use ^ 1)) {
+      int64_t c = 0;  // chunk = one 8-deep K step
+      for (int64_t kt = 0; kt < ktiles && ok; ++kt) {
+        const int s = (int)(kt % S);
+        const uint32_t ph = (uint32_t)((kt / S) & 1);
+        if (!mbar_wait(&sm.full[s], ph)) {
           ok = false;
           break;
         }
         fence_after();
-        const uint32_t d1 = tmem + (uint32_t)b * 192, d2 = d1 + 64, d3 = d1 + 128;
-        for (int t = 0; t < kChunkTiles && kt < ktiles; ++t, ++kt) {
-          const int s = (int)(kt % S);
-          const uint32_t ph = (uint32_t)((kt / S) & 1);
-          if (!mbar_wait(&sm.full[s], ph)) {
+        const uint32_t sa = smem_u32(sm.stage[s]);
+        const uint32_t sb = sa + P * kATile * 4;
+#pragma unroll
+        for (int j = 0; j < TK / 8; ++j, ++c) {
+          const int b = (int)(c & 1);
+          const uint32_t use = (uint32_t)((c >> 1) & 1);
+          if (!mbar_wait(&sm.acce[b], use ^ 1)) {
             ok = false;
             break;
           }
           fence_after();
-          const uint32_t sa = smem_u32(sm.stage[s]);
-          const uint32_t sb = sa + P * kATile * 4;
+          const uint32_t d1 = tmem + (uint32_t)b * 256, d2 = d1 + 64, d3 = d1 + 128, d4 = d1 + 192;
+          const uint32_t oa = (uint32_t)j * 2 * ALBO, ob = (uint32_t)j * 2 * BLBO;
+          // The tensor core rounds an accumulation toward zero.  The small
+          // correction products go in first (the first one overwrites), the
+          // large hi x hi product last, so each accumulator takes exactly one
+          // rounding at its full magnitude per chunk.
 #pragma unroll
-          for (int j = 0; j < TK / 8; ++j) {
-            const uint32_t oa = (uint32_t)j * 2 * ALBO, ob = (uint32_t)j * 2 * BLBO;
-            uint32_t acc = (t == 0 && j == 0) ? 0u : 1u;
-#pragma unroll
-            for (int q = 0; q < CF::products; ++q) {
-              // term pairs (i, j) with i + j < NS: (0,0) (0,1) (1,0) (0,2) (2,0) (1,1)
-              const int ti = (q == 2) ? 1 : (q == 4) ? 2 : (q == 5) ? 1 : 0;
-              const int tj = (q == 1) ? 1 : (q == 3) ? 2 : (q == 5) ? 1 : 0;
-              const uint64_t ar = smem_desc(sa + (0 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
-              const uint64_t ai = smem_desc(sa + (1 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
-              const uint64_t br = smem_desc(sb + (0 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
-              const uint64_t bi = smem_desc(sb + (1 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
-              mma_tf32(d1, ar, br, idesc, acc);
-              mma_tf32(d2, ai, bi, idesc, acc);
-              mma_tf32(d3, ar, bi, idesc, acc);
-              mma_tf32(d3, ai, br, idesc, 1u);
-              acc = 1u;
-            }
+          for (int q = 1; q <= CF::products; ++q) {
+            const int qq = q == CF::products ? 0 : q;  // hi x hi last
+            // term pairs (i, j) with i + j < NS: (0,0) (0,1) (1,0) (0,2) (2,0) (1,1)
+            const int ti = (qq == 2) ? 1 : (qq == 4) ? 2 : (qq == 5) ? 1 : 0;
+            const int tj = (qq == 1) ? 1 : (qq == 3) ? 2 : (qq == 5) ? 1 : 0;
+            const uint32_t acc = q == 1 ? 0u : 1u;
+            const uint64_t ar = smem_desc(sa + (0 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
+            const uint64_t ai = smem_desc(sa + (1 * NS + ti) * kATile * 4 + oa, ALBO, SBO);
+            const uint64_t br = smem_desc(sb + (0 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
+            const uint64_t bi = smem_desc(sb + (1 * NS + tj) * kBTile * 4 + ob, BLBO, SBO);
+            mma_tf32(d1, ar, br, idesc, acc);  // Ar.Br
+            mma_tf32(d2, ai, bi, idesc, acc);  // Ai.Bi
+            mma_tf32(d3, ar, bi, idesc, acc);  // Ar.Bi
+            mma_tf32(d4, ai, br, idesc, acc);  // Ai.Br
           }
-          mma_commit(&sm.empty[s]);  // smem stage free once these MMAs finish
+          mma_commit(&sm.accf[b]);  // chunk accumulators ready for the epilogue
         }
-        mma_commit(&sm.accf[b]);  // chunk accumulators ready for the epilogue
+        mma_commit(&sm.empty[s]);  // smem stage free once these MMAs finish
       }
     }
   } else {
@@ -352,14 +353,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       fence_after();
 #pragma unroll
       for (int piece = 0; piece < 4; ++piece) {
-        const uint32_t col = (uint32_t)(b * 192 + h * 32 + piece * 8);
-        float p1[8], p2[8], p3[8];
+        const uint32_t col = (uint32_t)(b * 256 + h * 32 + piece * 8);
+        float p1[8], p2[8], p3[8], p4[8];
         tmem_ld8(lane_base + col, p1);
         tmem_ld8(lane_base + col + 64, p2);
         tmem_ld8(lane_base + col + 128, p3);
+        tmem_ld8(lane_base + col + 192, p4);
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) kahan_add(acc[piece * 8 + j], make_float2(p1[j] - p2[j], p3[j]));
+        for (int j = 0; j < 8; ++j) kahan_add(acc[piece * 8 + j], make_float2(p1[j] - p2[j], p3[j] + p4[j]));
       }
       fence_before();
       __syncwarp();
