@@ -48,6 +48,9 @@ constexpr int kThreads = 320;
 constexpr uint32_t kTmemCols = 512;            // 2 sets x 4 accumulators x 64 columns
 constexpr uint32_t kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 constexpr int kStatusTcTimeout = 0x7c01;
+// Expected relative shrinkage of a value truncated (rounded toward zero) to
+// FP32: half an ulp over a log-uniform mantissa, 2^-24 * ln 2.
+constexpr float kTruncBias = 4.13145e-8f;
 constexpr int kATile = TM * TK;                // floats per A plane tile (8 KiB)
 constexpr int kBTile = TN * TK;                // floats per B plane tile (4 KiB)
 
@@ -361,7 +364,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_ld8(lane_base + col + 192, p4);
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) kahan_add(acc[piece * 8 + j], make_float2(p1[j] - p2[j], p3[j] + p4[j]));
+        for (int j = 0; j < 8; ++j) {
+          const float2 v = make_float2(p1[j] - p2[j], p3[j] + p4[j]);
+          kahan_add(acc[piece * 8 + j], v);
+          // The chunk value came out of one round-toward-zero at full
+          // magnitude, which shrinks it by 2^-24 ln 2 relative on average
+          // (mantissas log-uniform within a binade); add that expectation back
+          // through the compensation term (the sum is s - c).
+          acc[piece * 8 + j].c.x = fmaf(-kTruncBias, v.x, acc[piece * 8 + j].c.x);
+          acc[piece * 8 + j].c.y = fmaf(-kTruncBias, v.y, acc[piece * 8 + j].c.y);
+        }
       }
       fence_before();
       __syncwarp();
