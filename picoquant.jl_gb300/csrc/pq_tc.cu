@@ -12,25 +12,27 @@
 //
 // k_tc_pack gathers an operand through its index map (any mode order, batch
 // modes) into 2*NS planes {re terms, im terms} laid out tile by tile; a tile is
-// ROWS (128 for A, 64 for B) x 16 K values in the canonical no-swizzle
+// ROWS (128 for A, 48 for B) x 16 K values in the canonical no-swizzle
 // K-major UMMA layout: 8-row x 16-byte core matrices (128 contiguous bytes),
 // row-adjacent core matrices 128 bytes apart, K-adjacent ones ROWS*16 bytes
 // apart.  One bulk copy moves one plane tile.  Rows and K beyond the operand
 // are zero.
 //
-// k_tc_gemm: one CTA per 128 x 64 output tile (x batch), 10 warps.
+// k_tc_gemm: one CTA per 128 x 48 output tile (x batch), 14 warps.
 //   warp 0   producer: cp.async.bulk of the 4*NS plane tiles of one K step
 //            into a shared-memory ring (mbarrier complete_tx);
-//   warp 1   allocates TMEM and issues tcgen05.mma (M=128, N=64, K=8); every
+//   warp 1   allocates TMEM and issues tcgen05.mma (M=128, N=48, K=8); every
 //            8-deep K step is one chunk, alternating between two sets of four
-//            64-column FP32 accumulators, committed to the epilogue per chunk;
-//   warps 2-9 epilogue: warp w reads TMEM lanes 32*(w%4).. and 32 of the 64
+//            48-column FP32 accumulators, committed to the epilogue per chunk;
+//   warps 2-13 epilogue: warp w reads TMEM lanes 32*(w%4).. and 16 of the 48
 //            columns, folds each chunk's (P1 - P2, P3 + P4) into Kahan sums,
 //            hands the accumulator set back, and finally scatters C through
 //            the result index map.
 // The tensor core rounds accumulations toward zero; each chunk takes one such
 // rounding at full magnitude (its hi x hi product is issued last) and chunks
-// are summed with compensation, which keeps the bias from growing with K.  Every mbarrier wait is bounded; on expiry the
+// are summed with compensation, which keeps the bias from growing with K; the
+// expected shrinkage of that rounding is added back in the final store.
+// Every mbarrier wait is bounded; on expiry the
 // kernel records an error in the context's status word and runs to the end
 // (TMEM is always released), so the host sees PQ_ERR_DEVICE, not a hang.
 #include <cuda_runtime.h>
@@ -43,16 +45,17 @@ namespace pq {
 
 namespace {
 
-constexpr int TM = 128, TN = 64, TK = 16;
-constexpr int kThreads = 320;
-constexpr uint32_t kTmemCols = 512;            // 2 sets x 4 accumulators x 64 columns
+constexpr int TM = 128, TN = 48, TK = 16;
+constexpr int kThreads = 448;                  // producer, MMA, 12 epilogue warps
+constexpr int kEpiWarps = 12;
+constexpr uint32_t kTmemCols = 512;            // 2 sets x 4 accumulators x 48 columns = 384 used
 constexpr uint32_t kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 constexpr int kStatusTcTimeout = 0x7c01;
 // Expected relative shrinkage of a value truncated (rounded toward zero) to
 // FP32: half an ulp over a log-uniform mantissa, 2^-24 * ln 2.
 constexpr float kTruncBias = 4.13145e-8f;
 constexpr int kATile = TM * TK;                // floats per A plane tile (8 KiB)
-constexpr int kBTile = TN * TK;                // floats per B plane tile (4 KiB)
+constexpr int kBTile = TN * TK;                // floats per B plane tile (3 KiB)
 
 template <int NS>
 struct Cfg {
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.accf[b], 1);
-      mbar_init(&sm.acce[b], 8);  // one arrival per epilogue warp
+      mbar_init(&sm.acce[b], kEpiWarps);  // one arrival per epilogue warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           fence_after();
-          const uint32_t d1 = tmem + (uint32_t)b * 256, d2 = d1 + 64, d3 = d1 + 128, d4 = d1 + 192;
+          const uint32_t d1 = tmem + (uint32_t)b * (4 * TN), d2 = d1 + TN, d3 = d1 + 2 * TN, d4 = d1 + 3 * TN;
           const uint32_t oa = (uint32_t)j * 2 * ALBO, ob = (uint32_t)j * 2 * BLBO;
           // The tensor core rounds an accumulation toward zero.  The small
           // correction products go in first (the first one overwrites), the
@@ -337,13 +340,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // epilogue: warp w reads TMEM lanes of quadrant w % 4, columns [32h, 32h+32)
+    // epilogue: warp w reads TMEM lanes of quadrant w % 4, columns [16h, 16h+16)
+    constexpr int CW = TN / (kEpiWarps / 4);  // columns per epilogue warp
     const int q = warp & 3, h = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-    KahanC acc[32];
+    KahanC acc[CW];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) kahan_init(acc[j]);
+    for (int j = 0; j < CW; ++j) kahan_init(acc[j]);
     for (int64_t c = 0; c < nchunks; ++c) {
       const int b = (int)(c & 1);
       const uint32_t use = (uint32_t)((c >> 1) & 1);
@@ -355,25 +359,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       fence_after();
 #pragma unroll
-      for (int piece = 0; piece < 4; ++piece) {
-        const uint32_t col = (uint32_t)(b * 256 + h * 32 + piece * 8);
+      for (int piece = 0; piece < CW / 8; ++piece) {
+        const uint32_t col = (uint32_t)(b * 4 * TN + h * CW + piece * 8);
         float p1[8], p2[8], p3[8], p4[8];
         tmem_ld8(lane_base + col, p1);
-        tmem_ld8(lane_base + col + 64, p2);
-        tmem_ld8(lane_base + col + 128, p3);
-        tmem_ld8(lane_base + col + 192, p4);
+        tmem_ld8(lane_base + col + TN, p2);
+        tmem_ld8(lane_base + col + 2 * TN, p3);
+        tmem_ld8(lane_base + col + 3 * TN, p4);
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const float2 v = make_float2(p1[j] - p2[j], p3[j] + p4[j]);
-          kahan_add(acc[piece * 8 + j], v);
-          // The chunk value came out of one round-toward-zero at full
-          // magnitude, which shrinks it by 2^-24 ln 2 relative on average
-          // (mantissas log-uniform within a binade); add that expectation back
-          // through the compensation term (the sum is s - c).
-          acc[piece * 8 + j].c.x = fmaf(-kTruncBias, v.x, acc[piece * 8 + j].c.x);
-          acc[piece * 8 + j].c.y = fmaf(-kTruncBias, v.y, acc[piece * 8 + j].c.y);
-        }
+        for (int j = 0; j < 8; ++j) kahan_add(acc[piece * 8 + j], make_float2(p1[j] - p2[j], p3[j] + p4[j]));
       }
       fence_before();
       __syncwarp();
@@ -384,9 +379,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int64_t zc = decode(z, d.nz, d.zdim, d.zsc);
       if (cmr >= 0) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int64_t cnj = sm.cn[h * 32 + j];
-          if (cnj >= 0) C[zc + cmr + cnj] = store_as<TC>(kahan_value(acc[j]));
+        for (int j = 0; j < CW; ++j) {
+          const int64_t cnj = sm.cn[h * CW + j];
+          if (cnj < 0) continue;
+          // every chunk value came out of one round-toward-zero at full
+          // magnitude, which shrinks it by 2^-24 ln 2 relative on average
+          // (mantissas log-uniform within a binade); the sum is linear in the
+          // chunks, so the expectation is added back once here
+          const float2 v = kahan_value(acc[j]);
+          C[zc + cmr + cnj] = store_as<TC>(make_float2(fmaf(kTruncBias, v.x, v.x), fmaf(kTruncBias, v.y, v.y)));
         }
       }
     }
