@@ -143,7 +143,7 @@ def main():
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
     ap.add_argument("--depth", type=int, default=16)
-    ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "6xtf32", "3xbf16", "c128"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "6xtf32", "ozaki", "3xbf16", "c128"])
     ap.add_argument("--batch", type=int, default=0, help="slices per launch (0: sized from memory)")
     ap.add_argument("--cpu-log2", type=float, default=31.0, help="log2 complex MACs of the CPU sample")
     ap.add_argument("--slice-target", type=float, default=28.0,
@@ -324,7 +324,7 @@ def run_gb300(args, world, rank):
         dist.init_process_group("nccl")
     dev = torch.cuda.current_device()
     peaks, peaks_kind = load_peaks()
-    prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "3xbf16": pq.PREC_3XBF16,
+    prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI, "3xbf16": pq.PREC_3XBF16,
                 "c128": pq.PREC_C128}
     prec_name = args.precision if args.precision != "auto" else "3xtf32"
     precision = prec_map[prec_name]
@@ -481,7 +481,8 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
         "metric": METRIC, "value": value, "unit": "amplitudes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"c64": "c64", "3xtf32": "c64(3xtf32)", "6xtf32": "c64(6xtf32)",
-                                                           "3xbf16": "c64(3xbf16)", "c128": "c128"}[prec_name],
+                                                           "ozaki": "c64(ozaki-bf16)", "3xbf16": "c64(3xbf16)",
+                                                           "c128": "c128"}[prec_name],
         "data": "synthetic (seeded random circuits)", "config": workload_config(args, rows, cols, depth),
         "precision": prec_name, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
         "cpu_baseline": {"value": cpu_val, "unit": "amplitudes/s", "cores": os.cpu_count(), "kind": "port",

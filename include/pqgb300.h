@@ -58,12 +58,20 @@ extern "C" {
  * PQ_PREC_3XBF16 : accepted; runs as PQ_PREC_C64 (no bf16 tensor-core class:
  *                  a bf16 hi/lo split cannot reach 1e-6 amplitude error).
  * PQ_PREC_6XTF32 : as PQ_PREC_3XTF32 with a hi+mid+lo TF32 split and 6
- *                  products (hh, hm, mh, hl, lh, mm) per real product.       */
+ *                  products (hh, hm, mh, hl, lh, mm) per real product.
+ * PQ_PREC_OZAKI  : as PQ_PREC_C64, but large GEMM-shaped contractions with
+ *                  K <= 512 run the Ozaki scheme on the tcgen05 tensor cores:
+ *                  rows of A / columns of B scaled by powers of two, cut into
+ *                  five 7-bit bf16 slices, the 15 slice products of level
+ *                  <= 4 accumulated in FP32 TMEM where levels 0 and 1 are
+ *                  exact; the result is rounded once.  Larger K runs as
+ *                  PQ_PREC_6XTF32.                                          */
 #define PQ_PREC_C128    0
 #define PQ_PREC_C64     1
 #define PQ_PREC_3XTF32  2
 #define PQ_PREC_3XBF16  3
 #define PQ_PREC_6XTF32  4
+#define PQ_PREC_OZAKI   5
 
 #define PQ_MAX_RANK 56
 

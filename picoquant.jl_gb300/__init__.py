@@ -7,7 +7,7 @@ The API keeps PicoQuant's names (Julia's ``!`` dropped):
 backend (the role of ``InteractiveBackend{T}``).  All numeric work runs in
 ``libpqgb300.so`` (CUDA, sm_103a); there is no CPU fallback.
 """
-from ._lib import (PQ_C64, PQ_C128, PQError, PREC_3XBF16, PREC_3XTF32, PREC_6XTF32, PREC_C64, PREC_C128)
+from ._lib import (PQ_C64, PQ_C128, PQError, PREC_3XBF16, PREC_3XTF32, PREC_6XTF32, PREC_C64, PREC_C128, PREC_OZAKI)
 from .backend import GB300Backend, Metrics, decompose_array, record_compute_costs, record_memory_costs
 from .circuits import (CX, CZ, SWAP, H, build_network, cphase, ghz_gates, grid_patterns, grid_shape, haar_su2,
                        operator_to_tensor, qft_gates, random_bitstrings, random_grid_gates)

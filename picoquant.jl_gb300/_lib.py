@@ -25,6 +25,7 @@ PREC_C64 = 1
 PREC_3XTF32 = 2
 PREC_3XBF16 = 3
 PREC_6XTF32 = 4
+PREC_OZAKI = 5
 
 PQ_MAX_RANK = 56
 

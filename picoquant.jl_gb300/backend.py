@@ -46,7 +46,7 @@ def record_memory_costs(backend, mem):
 
 
 _PREC_NAMES = {L.PREC_C128: "c128", L.PREC_C64: "c64", L.PREC_3XTF32: "3xtf32", L.PREC_3XBF16: "3xbf16",
-               L.PREC_6XTF32: "6xtf32"}
+               L.PREC_6XTF32: "6xtf32", L.PREC_OZAKI: "ozaki"}
 
 
 class GB300Backend:
@@ -55,8 +55,10 @@ class GB300Backend:
     ``precision`` selects storage and arithmetic (the role of the element type
     ``T`` of ``InteractiveBackend{T}``): PREC_C128 (ComplexF64, FP64 math),
     PREC_C64 (ComplexF32 storage and FP32 math for large tensors),
-    PREC_3XTF32 / PREC_3XBF16 (as PREC_C64, with split-precision tensor-core
-    products for large pairs).  In the complex64 modes tensors of at most
+    PREC_3XTF32 / PREC_6XTF32 (as PREC_C64, with split-precision TF32
+    tensor-core products for large pairs), PREC_OZAKI (as PREC_C64, with
+    exact-accumulation bf16-slice tensor-core products for large pairs),
+    PREC_3XBF16 (accepted, runs as PREC_C64).  In the complex64 modes tensors of at most
     ``small_elems`` elements (default 65536) stay complex128: gate tensors and
     small intermediates cost nothing in time, and rounding them would dominate
     the error of the final amplitudes.

@@ -115,7 +115,7 @@ extern "C" {
 int pq_ctx_create(int device, int precision, pq_ctx** out) {
   if (!out) return PQ_ERR_INVALID;
   *out = nullptr;
-  if (precision < PQ_PREC_C128 || precision > PQ_PREC_6XTF32) return PQ_ERR_INVALID;
+  if (precision < PQ_PREC_C128 || precision > PQ_PREC_OZAKI) return PQ_ERR_INVALID;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return PQ_ERR_CUDA;
   pq_ctx* c = new pq_ctx();
@@ -332,7 +332,7 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
     }
     e = launch_tc(ctx->precision, A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, scratch, sbytes,
                   ctx->d_status, ctx->stream);
-    ctx->launches += 3;
+    ctx->launches += tc_launch_count(ctx->precision, pp.m);
   } else if (pp.kclass == KC_GEMM) {
     e = launch_gemm(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
     ctx->launches += 1;

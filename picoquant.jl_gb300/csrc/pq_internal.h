@@ -147,6 +147,13 @@ cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, cons
                       const GemmDesc& d, void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream);
 size_t tc_scratch_bytes(int precision, const GemmDesc& d);
 bool tc_eligible(int precision, const GemmDesc& d);
+int tc_launch_count(int precision, const GemmDesc& d);  // kernels one launch_tc issues
+// Exact-accumulation (Ozaki scheme, bf16 slices) tensor-core contraction
+// (pq_oz.cu), used by launch_tc for PQ_PREC_OZAKI when K <= 512.
+bool oz_eligible(const GemmDesc& d);
+size_t oz_scratch_bytes(const GemmDesc& d);
+cudaError_t launch_oz(int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
+                      void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream);
 
 }  // namespace pq
 

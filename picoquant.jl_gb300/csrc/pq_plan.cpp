@@ -290,7 +290,7 @@ bool compile(const Ctx* ctx, const std::vector<std::vector<int>>& leaf_labels,
     const PairPlan& p = tmp[idx].pp;
     cp.cmacs += (double)p.csize * (double)p.ksize;
     cp.max_elems = std::max(cp.max_elems, p.csize);
-    cp.launches += (p.kclass == KC_TC) ? 3 : 1;
+    cp.launches += (p.kclass == KC_TC) ? tc_launch_count(ctx->precision, p.m) : 1;
   }
   size_t sb = 0;
   for (auto& s : cp.steps)
@@ -310,7 +310,7 @@ bool compile(const Ctx* ctx, const std::vector<std::vector<int>>& leaf_labels,
 
 cudaError_t run_step(pq_plan* p, const Step& s, const void* A, const void* B, void* C) {
   Ctx* ctx = p->ctx;
-  ctx->launches += (s.pp.kclass == KC_TC) ? 3 : 1;
+  ctx->launches += (s.pp.kclass == KC_TC) ? tc_launch_count(ctx->precision, s.pp.m) : 1;
   if (s.is_copy) return launch_permute(s.ta, s.tc, A, 0, C, s.pp.g, ctx->stream);
   switch (s.pp.kclass) {
     case KC_TC:
