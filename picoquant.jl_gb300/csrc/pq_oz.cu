@@ -31,25 +31,38 @@
 //   Cr = Ar.Br + (-Ai).Bi   (the negation is the MMA's negate-A bit)
 //   Ci = Ar.Bi + Ai.Br
 //
+// Complex arithmetic on real tensor cores: a tile of 64 complex rows of A is
+// held as the 192-row stack [Ar; Ai; -Ar] of each slice, so that
+//   X1 = rows 0..127   = [Ar; Ai]
+//   X2 = rows 64..191  = [Ai; -Ar]  (issued with the MMA's negate-A bit: [-Ai; Ar])
+// and one accumulator of 128 TMEM lanes receives
+//   X1 . Br + X2' . Bi = [Ar.Br - Ai.Bi ; Ai.Br + Ar.Bi] = [Cr ; Ci]
+// for the 64 rows: 2 MMAs (M=128, N=TN, K=16) per slice pair and K tile.
+//
 // Kernels (one launch each, in stream order):
-//   k_oz_exp      row / column scale exponents of A and B
-//   k_oz_pack     slices into planes [z][row tile][k tile][plane][ROWS*16 bf16]
-//                 in the canonical no-swizzle K-major UMMA layout (8-row x
-//                 16-byte core matrices: 8 rows x 8 bf16), planes
-//                 {Re s0..s4, Im s0..s4}; rows and K beyond the operand are 0
-//   k_result_index result offsets of every row and column of C
-//   k_oz_gemm     persistent, one CTA per SM over 128 x TN output tiles (TN =
-//                 64, or 32 / 16 for narrow pairs; a pair whose A side is the
-//                 narrow one runs as B x A):
-//     warp 0     producer: cp.async.bulk of the 20 plane tiles of one 16-deep
-//                K tile into a 3- or 4-stage shared-memory ring;
-//     warp 1     TMEM owner and MMA issuer: 60 tcgen05.mma (kind::f16, bf16,
-//                M=128, N=TN, K=16) per K tile into six TN-column
-//                accumulators (L0r L0i L1r L1i L2r L2i);
-//     warps 2-9  epilogue, once per tile: warp w reads TMEM lanes 32*(w%4)..
-//                and half of the TN columns, combines the levels with an
-//                error-free two-sum, scales by 2^(ea+eb) and scatters C
-//                through the result index map.
+//   k_oz_exp        row scale exponents of A, column scale exponents of B
+//   k_oz_pack       B's slices into planes [z][col tile][k tile][plane][TN*16
+//                   bf16] in the canonical no-swizzle K-major UMMA layout
+//                   (8-row x 16-byte core matrices), planes {Re s0..s4, Im
+//                   s0..s4}; columns and K beyond the operand are 0
+//   k_result_index  result offsets of every row and column of C
+//   k_oz_gemm       persistent, one CTA per SM over 64 x TN complex output
+//                   tiles (TN = 128, or 64 / 32 / 16 for narrow pairs; a pair
+//                   whose A side is the narrow one runs as B x A):
+//     warp 0       producer: cp.async.bulk of B's 10 plane tiles of one
+//                  16-deep K tile into the shared-memory ring;
+//     warp 1       TMEM owner and MMA issuer: 30 tcgen05.mma (kind::f16,
+//                  bf16) per K tile into three TN-column accumulators (levels
+//                  0, 1, 2-4);
+//     warps 2-9    A converters: gather A's 64 x 16 complex values of the K
+//                  tile through its index map straight from HBM (the next K
+//                  tile's loads in flight while this one is sliced), slice
+//                  them and store the [Ar; Ai; -Ar] stacks into the ring (no
+//                  slice planes of A ever reach HBM);
+//     warps 10-17  epilogue, once per tile: Cr from TMEM lanes 0-63, Ci from
+//                  lanes 64-127; the levels are combined with an error-free
+//                  two-sum, scaled by 2^(ea+eb) and scattered through the
+//                  result index map.
 // Every mbarrier wait is bounded; on expiry the kernel records an error in the
 // context's status word and runs to the end (TMEM is always released).
 #include <cuda_bf16.h>
@@ -67,26 +80,28 @@ namespace {
 
 using namespace tcg;
 
-constexpr int TM = 128, TK = 16;
+constexpr int TK = 16;
 constexpr int kSlices = 5;                       // bf16 slices per real value
 constexpr int kPlanes = 2 * kSlices;             // per operand: Re s0..s4, Im s0..s4
 constexpr int kPairs = 15;                       // slice pairs (i, j) with i + j <= 4
-constexpr int kThreads = 320;                    // producer, MMA, 8 epilogue warps
-constexpr int kEpiWarps = 8;
-constexpr int kATile = TM * TK;                  // bf16 per A plane tile (4 KiB)
+constexpr int kThreads = 576;                    // producer, MMA, 8 converter + 8 epilogue warps
+constexpr int kConvWarps = 8, kEpiWarps = 8;
+constexpr int kRows = 64;                        // complex rows of A per tile
+constexpr int kStackBytes = 3 * kRows * TK * 2;  // one slice's [Ar; Ai; -Ar] stack (6 KiB)
+constexpr int kExpZero = -4096;                  // exponent of an all-zero row
+constexpr int64_t kMaxK = 512;                   // exact level-0/1 sums up to this K
 
-// Tile width N: 64 for general pairs, 32 and 16 for narrow ones.
+// Tile width N: 128 for general pairs, 64 / 32 / 16 for narrow ones.
 template <int TN>
 struct OzCfg {
   static constexpr int kBTile = TN * TK;                                   // bf16 per B plane tile
-  static constexpr uint32_t stage_bytes = kPlanes * (kATile + kBTile) * 2;
-  static constexpr int stages = TN == 64 ? 3 : 4;
-  static constexpr uint32_t tmem_cols = TN == 64 ? 512 : (TN == 32 ? 256 : 128);  // >= 6 TN, power of 2
-  static constexpr int cw = TN / (kEpiWarps / 4);                           // columns per epilogue warp
-  static_assert(6 * TN <= (int)tmem_cols && cw % 8 == 0, "tile width");
+  static constexpr uint32_t b_bytes = kPlanes * kBTile * 2;                // B planes of one K tile
+  static constexpr uint32_t stage_bytes = kSlices * kStackBytes + b_bytes;
+  static constexpr int stages = TN == 128 ? 3 : 4;
+  static constexpr uint32_t tmem_cols = TN == 128 ? 512 : (TN == 64 ? 256 : (TN == 32 ? 128 : 64));
+  static constexpr int cw = TN / 2;                                         // columns per epilogue warp
+  static_assert(3 * TN <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
 };
-constexpr int kExpZero = -4096;                  // exponent of an all-zero row
-constexpr int64_t kMaxK = 512;                   // exact level-0/1 sums up to this K
 
 // slice pairs, level 0 first, then level 1, then levels 4, 3, 2 (the inexact
 // accumulator takes its small terms first)
@@ -172,15 +187,29 @@ __global__ void __launch_bounds__(256) k_oz_exp(const T* __restrict__ X, const _
 template <typename R>
 __device__ __forceinline__ void slices(R x, float* s) {
   R r = x;
-  R g = (R)128.0;  // 2^7(i+1)
+  R g = (R)128.0, gi = (R)(1.0 / 128.0);  // 2^7(i+1) and its inverse (exact)
 #pragma unroll
   for (int i = 0; i < kSlices; ++i) {
-    const R si = round_int(r * g) / g;
+    const R si = round_int(r * g) * gi;
     s[i] = (float)si;
     r -= si;
     g *= (R)128.0;
+    gi *= (R)(1.0 / 128.0);
   }
 }
+
+// 2^k as a float for -126 <= k <= 127.
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+// Two factors whose product is 2^-e (|e| <= 252), each a normal float: x 2^-e
+// is (x f.x) f.y, exact unless the result underflows (far below any slice).
+__device__ __forceinline__ float2 inv_scale(int e) {
+  const int a = (-e) / 2;
+  return make_float2(pow2f(a), pow2f(-e - a));
+}
+// x 2^-e: complex64 rows (|e| <= 149) by the two factors f, complex128 rows
+// (any exponent) by ldexp.
+__device__ __forceinline__ float scale_row(float x, int, float2 f) { return (x * f.x) * f.y; }
+__device__ __forceinline__ double scale_row(double x, int e, float2) { return ldexp(x, -e); }
 
 template <typename T, int ROWS>
 __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_bfloat16* __restrict__ planes,
@@ -233,7 +262,8 @@ __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_b
 
 template <int TN>
 struct alignas(1024) OzSmem {
-  __nv_bfloat16 stage[OzCfg<TN>::stages][kPlanes * (kATile + OzCfg<TN>::kBTile)];  // A planes, then B planes
+  unsigned char stage[OzCfg<TN>::stages][OzCfg<TN>::stage_bytes];  // A stacks, then B planes
+  int64_t koff[kMaxK];                                              // A's K offsets
   uint64_t full[OzCfg<TN>::stages];
   uint64_t empty[OzCfg<TN>::stages];
   uint64_t accf;
@@ -258,14 +288,24 @@ __device__ __forceinline__ double combine(float l0, float l1, float l2, int ex, 
   return ldexp(((double)l0 + (double)l1) + (double)l2, ex);
 }
 
-template <typename TC, int TN>
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // exact: slices have <= 8 bits
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ void sts64(uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
+}
+// Generic-proxy shared-memory writes made visible to the tensor core's reads.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+template <typename TA, typename TC, int TN>
 __global__ void __launch_bounds__(kThreads, 1)
-    k_oz_gemm(const __nv_bfloat16* __restrict__ pa, const __nv_bfloat16* __restrict__ pb, TC* __restrict__ C,
+    k_oz_gemm(const TA* __restrict__ A, const __nv_bfloat16* __restrict__ pb, TC* __restrict__ C,
               const __grid_constant__ GemmDesc d, const int64_t* __restrict__ cm_tab,
               const int64_t* __restrict__ cn_tab, const int* __restrict__ ea, const int* __restrict__ eb,
               int64_t mtiles, int64_t ntiles, int64_t ktiles, int* status) {
   using CF = OzCfg<TN>;
-  constexpr int kStages = CF::stages, kBTile = CF::kBTile;
+  constexpr int kStages = CF::stages;
   constexpr uint32_t kTmemCols = CF::tmem_cols;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   OzSmem<TN>& sm = *reinterpret_cast<OzSmem<TN>*>(smem_raw);
@@ -274,7 +314,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.full[s], 1 + kConvWarps);  // producer's expect_tx + one arrival per converter warp
       mbar_init(&sm.empty[s], 1);
     }
     mbar_init(&sm.accf, 1);
@@ -282,6 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(&sm.drain, 1);
     mbar_init_fence();
   }
+  for (int t = threadIdx.x; t < d.K; t += blockDim.x) sm.koff[t] = decode(t, d.nk, d.kdim, d.ksa);
   if (warp == 1) tmem_alloc(&sm.tmem_base, kTmemCols);
   fence_before();
   __syncthreads();
@@ -293,9 +334,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int64_t g = 0;  // K tiles issued so far (all tiles)
       for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x) {
-        const int64_t nt = tile % ntiles, r = tile / ntiles, mt = r % mtiles, z = r / mtiles;
-        const __nv_bfloat16* atile = pa + ((z * mtiles + mt) * ktiles) * (int64_t)(kPlanes * kATile);
-        const __nv_bfloat16* btile = pb + ((z * ntiles + nt) * ktiles) * (int64_t)(kPlanes * kBTile);
+        const int64_t nt = tile % ntiles, z = tile / (ntiles * mtiles);
+        const __nv_bfloat16* btile = pb + ((z * ntiles + nt) * ktiles) * (int64_t)(kPlanes * CF::kBTile);
         for (int64_t kt = 0; kt < ktiles; ++kt, ++g) {
           const int s = (int)(g % kStages);
           const uint32_t ph = (uint32_t)((g / kStages) & 1);
@@ -303,15 +343,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             ok = false;
             break;
           }
-          mbar_expect_tx(&sm.full[s], CF::stage_bytes);
-          const __nv_bfloat16* a = atile + kt * (kPlanes * kATile);
-          const __nv_bfloat16* b = btile + kt * (kPlanes * kBTile);
-          __nv_bfloat16* dst = sm.stage[s];
-#pragma unroll
-          for (int p = 0; p < kPlanes; ++p) {
-            bulk_g2s(dst + p * kATile, a + p * kATile, kATile * 2, &sm.full[s]);
-            bulk_g2s(dst + kPlanes * kATile + p * kBTile, b + p * kBTile, kBTile * 2, &sm.full[s]);
-          }
+          mbar_expect_tx(&sm.full[s], CF::b_bytes);
+          bulk_g2s(sm.stage[s] + kSlices * kStackBytes, btile + kt * (kPlanes * CF::kBTile), CF::b_bytes,
+                   &sm.full[s]);
         }
       }
       // the copies of the last stages are in flight until their full barrier
@@ -321,8 +355,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16(TM, TN), idesc_neg = idesc_bf16(TM, TN, true);
-      constexpr uint32_t ALBO = (TM / 8) * 128, BLBO = (TN / 8) * 128, SBO = 128;
+      constexpr uint32_t idesc = idesc_bf16(128, TN), idesc_neg = idesc_bf16(128, TN, true);
+      constexpr uint32_t ALBO = 24 * 128, BLBO = (TN / 8) * 128, SBO = 128;
       int64_t g = 0;  // K tiles consumed so far
       int64_t t = 0;  // tiles of this CTA
       for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
@@ -342,20 +376,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           fence_after();
           const uint32_t sa = smem_u32(sm.stage[s]);
           const uint64_t a0 = smem_desc(sa, ALBO, SBO);
-          const uint64_t b0 = smem_desc(sa + kPlanes * kATile * 2, BLBO, SBO);
+          const uint64_t b0 = smem_desc(sa + kSlices * kStackBytes, BLBO, SBO);
 #pragma unroll
           for (int p = 0; p < kPairs; ++p) {
             const int i = pair_i(p), j = pair_j(p);
             const uint32_t acc = (kt == 0 && first_of_level(p)) ? 0u : 1u;
-            const uint32_t dr = tmem + (uint32_t)(level_of(p) * 2 * TN), di = dr + TN;
-            const uint64_t ar = a0 + (uint64_t)(((0 * kSlices + i) * kATile * 2) >> 4);
-            const uint64_t ai = a0 + (uint64_t)(((1 * kSlices + i) * kATile * 2) >> 4);
-            const uint64_t br = b0 + (uint64_t)(((0 * kSlices + j) * kBTile * 2) >> 4);
-            const uint64_t bi = b0 + (uint64_t)(((1 * kSlices + j) * kBTile * 2) >> 4);
-            mma_bf16(dr, ar, br, idesc, acc);     // + Ar.Br
-            mma_bf16(di, ar, bi, idesc, acc);     // + Ar.Bi
-            mma_bf16(dr, ai, bi, idesc_neg, 1u);  // - Ai.Bi
-            mma_bf16(di, ai, br, idesc, 1u);      // + Ai.Br
+            const uint32_t dl = tmem + (uint32_t)(level_of(p) * TN);
+            const uint64_t x1 = a0 + (uint64_t)((i * kStackBytes) >> 4);             // [Ar; Ai]
+            const uint64_t x2 = a0 + (uint64_t)((i * kStackBytes + 8 * 128) >> 4);   // [Ai; -Ar]
+            const uint64_t br = b0 + (uint64_t)(((0 * kSlices + j) * CF::kBTile * 2) >> 4);
+            const uint64_t bi = b0 + (uint64_t)(((1 * kSlices + j) * CF::kBTile * 2) >> 4);
+            mma_bf16(dl, x1, br, idesc, acc);     // [Ar.Br ; Ai.Br]
+            mma_bf16(dl, x2, bi, idesc_neg, 1u);  // [-Ai.Bi ; Ar.Bi]
           }
           mma_commit(&sm.empty[s]);  // smem stage free once these MMAs finish
         }
@@ -366,16 +398,91 @@ __global__ void __launch_bounds__(kThreads, 1)
       mma_commit(&sm.drain);
       if (!mbar_wait(&sm.drain, 0)) ok = false;
     }
+  } else if (warp < 2 + kConvWarps) {
+    // converters: thread c handles row r = c % 64 and the 4 K values
+    // [4q, 4q+4) of every K tile (half of a 16-byte core-matrix row per
+    // stack block)
+    const int c = threadIdx.x - 64;
+    const int r = c & (kRows - 1), qd = c >> 6;
+    using R = typename Real<TA>::R;
+    // byte offset of (slice 0, block 0, row r, K quarter qd) in the stacks
+    const uint32_t row_off = (uint32_t)((((qd >> 1) * 24 + (r >> 3)) * 8 + (r & 7)) * 16 + (qd & 1) * 8);
+    int64_t g = 0;
+    for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x) {
+      const int64_t rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
+      const int64_t m = mt * kRows + r;
+      const bool mrow = m < d.M;
+      const int e = mrow ? ea[z * d.M + m] : kExpZero;
+      const bool live = mrow && e != kExpZero;
+      const float2 f = inv_scale(live ? e : 0);
+      const TA* arow = A + (live ? decode(z, d.nz, d.zdim, d.zsa) + decode(m, d.nm, d.mdim, d.msa) : 0);
+      auto load = [&](int64_t kt, TA* v) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int64_t k = kt * TK + qd * 4 + q;
+          if (live && k < d.K) {
+            v[q] = arow[sm.koff[k]];
+          } else {
+            v[q].x = 0;
+            v[q].y = 0;
+          }
+        }
+      };
+      TA nxt[4];
+      load(0, nxt);
+      for (int64_t kt = 0; kt < ktiles; ++kt, ++g) {
+        const int s = (int)(g % kStages);
+        const uint32_t ph = (uint32_t)((g / kStages) & 1);
+        TA cur[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
+        if (kt + 1 < ktiles) load(kt + 1, nxt);  // in flight while this tile is sliced
+        float re[kSlices][4], im[kSlices][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float a[kSlices], b[kSlices];
+          slices<R>(scale_row((R)cur[q].x, e, f), a);
+          slices<R>(scale_row((R)cur[q].y, e, f), b);
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i) {
+            re[i][q] = a[i];
+            im[i][q] = b[i];
+          }
+        }
+        bool got = mbar_wait(&sm.empty[s], ph ^ 1);
+        got = __all_sync(0xffffffffu, got);
+        if (!got) {
+          ok = false;
+          break;
+        }
+        const uint32_t base = smem_u32(sm.stage[s]) + row_off;
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          const uint32_t r0 = pack_bf16x2(re[i][0], re[i][1]), r1 = pack_bf16x2(re[i][2], re[i][3]);
+          const uint32_t i0 = pack_bf16x2(im[i][0], im[i][1]), i1 = pack_bf16x2(im[i][2], im[i][3]);
+          const uint32_t slice = base + (uint32_t)(i * kStackBytes);
+          sts64(slice, r0, r1);                                           // Ar
+          sts64(slice + 8 * 128, i0, i1);                                 // Ai
+          sts64(slice + 16 * 128, r0 ^ 0x80008000u, r1 ^ 0x80008000u);   // -Ar
+        }
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.full[s]);
+      }
+    }
   } else {
-    // epilogue: warp w reads TMEM lanes of quadrant w % 4, columns [32h, 32h+32)
+    // epilogue: warp w reads TMEM lanes of quadrant w % 4 (0, 1: Cr of rows
+    // 0..63; 2, 3: Ci), columns [h TN/2, (h+1) TN/2)
     constexpr int CW = CF::cw;
-    const int q = warp & 3, h = (warp - 2) >> 2;
-    const int row = q * 32 + lane;
+    const int q = warp & 3, h = (warp - 2 - kConvWarps) >> 2;
+    const int part = q >> 1;               // 0: real parts, 1: imaginary parts
+    const int r = (q & 1) * 32 + lane;     // complex row within the tile
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
     using R = typename std::conditional<std::is_same<TC, double2>::value, double, float>::type;
+    R* Cr = reinterpret_cast<R*>(C);
     int64_t t = 0;
     for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
-      const int64_t nt = tile % ntiles, r = tile / ntiles, mt = r % mtiles, z = r / mtiles;
+      const int64_t nt = tile % ntiles, rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
       bool got = mbar_wait(&sm.accf, (uint32_t)(t & 1));
       got = __all_sync(0xffffffffu, got);  // the TMEM loads below are warp-collective
       if (!got) {
@@ -383,21 +490,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       fence_after();
-      const int64_t m = mt * TM + row;
+      const int64_t m = mt * kRows + r;
       const bool mrow = m < d.M;
       const int64_t base = mrow ? decode(z, d.nz, d.zdim, d.zsc) + cm_tab[m] : 0;
-      const int exa = mrow ? ea[z * d.M + m] : 0;
+      const int exa = mrow ? ea[z * d.M + m] : kExpZero;
 #pragma unroll 1
       for (int piece = 0; piece < CW / 8; ++piece) {
         __syncwarp();  // the TMEM loads are warp-collective
         const uint32_t col = (uint32_t)(h * CW + piece * 8);
-        float l0r[8], l0i[8], l1r[8], l1i[8], l2r[8], l2i[8];
-        tmem_ld8(lane_base + col + 0 * TN, l0r);
-        tmem_ld8(lane_base + col + 1 * TN, l0i);
-        tmem_ld8(lane_base + col + 2 * TN, l1r);
-        tmem_ld8(lane_base + col + 3 * TN, l1i);
-        tmem_ld8(lane_base + col + 4 * TN, l2r);
-        tmem_ld8(lane_base + col + 5 * TN, l2i);
+        float l0[8], l1[8], l2[8];
+        tmem_ld8(lane_base + col + 0 * TN, l0);
+        tmem_ld8(lane_base + col + 1 * TN, l1);
+        tmem_ld8(lane_base + col + 2 * TN, l2);
         tmem_wait_ld();
         if (piece == CW / 8 - 1) {  // every value of this tile is in registers
           fence_before();
@@ -409,17 +513,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int j = 0; j < 8; ++j) {
           if (!mrow || n0 + j >= d.N) break;
           const int ex = exa + eb[z * d.N + n0 + j];
-          R vr, vi;
-          if (exa == kExpZero || ex < -2 * 1100) {
-            vr = vi = (R)0;  // an all-zero row or column
-          } else {
-            vr = combine(l0r[j], l1r[j], l2r[j], ex, R());
-            vi = combine(l0i[j], l1i[j], l2i[j], ex, R());
-          }
-          TC out;
-          out.x = vr;
-          out.y = vi;
-          C[base + cn_tab[n0 + j]] = out;
+          const R v = (exa == kExpZero || ex < -2 * 1100) ? (R)0 : combine(l0[j], l1[j], l2[j], ex, R());
+          Cr[2 * (base + cn_tab[n0 + j]) + part] = v;
         }
       }
     }
@@ -433,23 +528,22 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-int oz_tile_n(int64_t n) { return n <= 16 ? 16 : (n <= 32 ? 32 : 64); }
+int oz_tile_n(int64_t n) { return n <= 16 ? 16 : (n <= 32 ? 32 : (n <= 64 ? 64 : 128)); }
 
 struct OzLayout {
   int tn;
   int64_t mt, nt, kt;
-  size_t pa, pb, cm, cn, ea, eb, total;  // byte offsets from the aligned base
+  size_t pb, cm, cn, ea, eb, total;  // byte offsets from the aligned base
 };
 
 OzLayout layout(const GemmDesc& d) {
   OzLayout L;
   L.tn = oz_tile_n(d.N);
-  L.mt = ceil_div(d.M, TM);
+  L.mt = ceil_div(d.M, kRows);
   L.nt = ceil_div(d.N, L.tn);
   L.kt = ceil_div(d.K, TK);
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  L.pa = 0;
-  L.pb = up(L.pa + (size_t)(d.Z * L.mt * L.kt) * kPlanes * kATile * 2);
+  L.pb = 0;
   L.cm = up(L.pb + (size_t)(d.Z * L.nt * L.kt) * kPlanes * (L.tn * TK) * 2);
   L.cn = up(L.cm + (size_t)d.M * 8);
   L.ea = up(L.cn + (size_t)d.N * 8);
@@ -458,8 +552,8 @@ OzLayout layout(const GemmDesc& d) {
   return L;
 }
 
-// The kernels keep the long side on M (the 128 TMEM lanes): a pair whose A
-// side is the narrow one is run as C = B x A with the roles swapped.
+// The kernels keep the long side on M (the TMEM lanes): a pair whose A side
+// is the narrow one is run as C = B x A with the roles swapped.
 GemmDesc swapped(const GemmDesc& d) {
   GemmDesc s = d;
   s.M = d.N;
@@ -483,53 +577,55 @@ GemmDesc swapped(const GemmDesc& d) {
 bool needs_swap(const GemmDesc& d) { return d.M < 64 && d.N > d.M; }
 
 template <typename T, int ROWS>
-void prep_rows(const void* X, int side, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
-               cudaStream_t s) {
-  const int64_t rows = side == 0 ? d.M : d.N;
-  k_oz_exp<T, ROWS><<<dim3((unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, d, side, rows, e);
-  k_oz_pack<T, ROWS><<<dim3((unsigned)kt, (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, planes, d, side,
-                                                                                       rows, rtiles, kt, e);
+void prep_b(const void* X, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
+            cudaStream_t s) {
+  k_oz_exp<T, ROWS><<<dim3((unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, d, 1, d.N, e);
+  k_oz_pack<T, ROWS><<<dim3((unsigned)kt, (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, planes, d, 1,
+                                                                                       d.N, rtiles, kt, e);
 }
 
 template <typename T>
-void prep_operand(const void* X, int side, int rows_per_tile, __nv_bfloat16* planes, int* e, const GemmDesc& d,
-                  int64_t rtiles, int64_t kt, cudaStream_t s) {
-  if (rows_per_tile == TM) prep_rows<T, TM>(X, side, planes, e, d, rtiles, kt, s);
-  else if (rows_per_tile == 64) prep_rows<T, 64>(X, side, planes, e, d, rtiles, kt, s);
-  else if (rows_per_tile == 32) prep_rows<T, 32>(X, side, planes, e, d, rtiles, kt, s);
-  else prep_rows<T, 16>(X, side, planes, e, d, rtiles, kt, s);
+void prep_b_tn(const void* X, int tn, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
+               cudaStream_t s) {
+  if (tn == 128) prep_b<T, 128>(X, planes, e, d, rtiles, kt, s);
+  else if (tn == 64) prep_b<T, 64>(X, planes, e, d, rtiles, kt, s);
+  else if (tn == 32) prep_b<T, 32>(X, planes, e, d, rtiles, kt, s);
+  else prep_b<T, 16>(X, planes, e, d, rtiles, kt, s);
 }
 
-template <typename TC, int TN>
-cudaError_t oz_gemm_launch(const __nv_bfloat16* pa, const __nv_bfloat16* pb, void* C, const GemmDesc& d,
-                           const int64_t* cm, const int64_t* cn, const int* ea, const int* eb, const OzLayout& L,
-                           int* status, cudaStream_t s) {
+template <typename TA, typename TC, int TN>
+cudaError_t oz_gemm_launch(const void* A, const __nv_bfloat16* pb, void* C, const GemmDesc& d, const int64_t* cm,
+                           const int64_t* cn, const int* ea, const int* eb, const OzLayout& L, int* status,
+                           cudaStream_t s) {
   static_assert(sizeof(OzSmem<TN>) + 1024 <= 232448, "shared memory layout exceeds 227 KiB");
   const size_t smem = sizeof(OzSmem<TN>) + 1024;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_oz_gemm<TC, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_oz_gemm<TA, TC, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   const int64_t tiles = L.mt * L.nt * d.Z;
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
-  k_oz_gemm<TC, TN><<<grid, kThreads, smem, s>>>(pa, pb, (TC*)C, d, cm, cn, ea, eb, L.mt, L.nt, L.kt, status);
+  k_oz_gemm<TA, TC, TN><<<grid, kThreads, smem, s>>>((const TA*)A, pb, (TC*)C, d, cm, cn, ea, eb, L.mt, L.nt, L.kt,
+                                                     status);
   return cudaGetLastError();
 }
 
-template <typename TC>
-cudaError_t oz_gemm_tn(const __nv_bfloat16* pa, const __nv_bfloat16* pb, void* C, const GemmDesc& d,
-                       const int64_t* cm, const int64_t* cn, const int* ea, const int* eb, const OzLayout& L,
-                       int* status, cudaStream_t s) {
-  if (L.tn == 64) return oz_gemm_launch<TC, 64>(pa, pb, C, d, cm, cn, ea, eb, L, status, s);
-  if (L.tn == 32) return oz_gemm_launch<TC, 32>(pa, pb, C, d, cm, cn, ea, eb, L, status, s);
-  return oz_gemm_launch<TC, 16>(pa, pb, C, d, cm, cn, ea, eb, L, status, s);
+template <typename TA, typename TC>
+cudaError_t oz_gemm_tn(const void* A, const __nv_bfloat16* pb, void* C, const GemmDesc& d, const int64_t* cm,
+                       const int64_t* cn, const int* ea, const int* eb, const OzLayout& L, int* status,
+                       cudaStream_t s) {
+  if (L.tn == 128) return oz_gemm_launch<TA, TC, 128>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  if (L.tn == 64) return oz_gemm_launch<TA, TC, 64>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  if (L.tn == 32) return oz_gemm_launch<TA, TC, 32>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  return oz_gemm_launch<TA, TC, 16>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
 }
 
 bool eligible_oriented(const GemmDesc& d) {
   if (d.M < 64 || d.N < 8 || d.K < 16 || d.K > kMaxK) return false;
-  if (d.Z > 65535 || ceil_div(d.M, TM) > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535) return false;
+  if (d.Z > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535 || ceil_div(d.M, 128) > 65535) return false;
   return layout(d).total <= (size_t(24) << 30);
 }
 
@@ -551,26 +647,30 @@ cudaError_t launch_oz(int ta, int tb, int tc, const void* A, const void* B, void
   const OzLayout L = layout(d);
   if (!scratch || scratch_bytes < L.total) return cudaErrorInvalidValue;
   char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
-  auto* pa = (__nv_bfloat16*)(base + L.pa);
   auto* pb = (__nv_bfloat16*)(base + L.pb);
   auto* cm = (int64_t*)(base + L.cm);
   auto* cn = (int64_t*)(base + L.cn);
   auto* ea = (int*)(base + L.ea);
   auto* eb = (int*)(base + L.eb);
   if (ta == PQ_C128)
-    prep_operand<double2>(A, 0, TM, pa, ea, d, L.mt, L.kt, stream);
+    k_oz_exp<double2, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, stream>>>(
+        (const double2*)A, d, 0, d.M, ea);
   else
-    prep_operand<float2>(A, 0, TM, pa, ea, d, L.mt, L.kt, stream);
+    k_oz_exp<float2, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, stream>>>(
+        (const float2*)A, d, 0, d.M, ea);
   if (tb == PQ_C128)
-    prep_operand<double2>(B, 1, L.tn, pb, eb, d, L.nt, L.kt, stream);
+    prep_b_tn<double2>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
   else
-    prep_operand<float2>(B, 1, L.tn, pb, eb, d, L.nt, L.kt, stream);
+    prep_b_tn<float2>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
   const int64_t idx_blocks = std::min<int64_t>(ceil_div(d.M + d.N, 256), 152 * 8);
   k_result_index<<<(unsigned)idx_blocks, 256, 0, stream>>>(d, cm, cn);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return tc == PQ_C128 ? oz_gemm_tn<double2>(pa, pb, C, d, cm, cn, ea, eb, L, status, stream)
-                       : oz_gemm_tn<float2>(pa, pb, C, d, cm, cn, ea, eb, L, status, stream);
+  if (ta == PQ_C128)
+    return tc == PQ_C128 ? oz_gemm_tn<double2, double2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
+                         : oz_gemm_tn<double2, float2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
+  return tc == PQ_C128 ? oz_gemm_tn<float2, double2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
+                       : oz_gemm_tn<float2, float2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
 }
 
 }  // namespace pq

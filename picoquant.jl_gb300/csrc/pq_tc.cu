@@ -391,9 +391,9 @@ bool tc_eligible(int precision, const GemmDesc& d) {
 }
 
 int tc_launch_count(int precision, const GemmDesc& d) {
-  // exponents + slices of A and B, result index table, GEMM; or the TF32
-  // path's index table, two packs, GEMM
-  return (precision == PQ_PREC_OZAKI && oz_eligible(d)) ? 6 : 4;
+  // exponents of A and B, slices of B, result index table, GEMM (A is sliced
+  // inside it); or the TF32 path's index table, two packs, GEMM
+  return (precision == PQ_PREC_OZAKI && oz_eligible(d)) ? 5 : 4;
 }
 
 cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
