@@ -326,7 +326,7 @@ def run_gb300(args, world, rank):
     peaks, peaks_kind = load_peaks()
     prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI, "3xbf16": pq.PREC_3XBF16,
                 "c128": pq.PREC_C128}
-    prec_name = args.precision if args.precision != "auto" else "3xtf32"
+    prec_name = args.precision if args.precision != "auto" else "ozaki"
     precision = prec_map[prec_name]
 
     if args.workload == "grid6x6_d16_sliced":

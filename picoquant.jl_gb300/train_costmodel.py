@@ -3,8 +3,10 @@ with the flop-count planner.
 
     python picoquant.jl_gb300/train_costmodel.py --pairs 200000 --out costmodel_gb300.npz
 
-Measures ``--pairs`` random complex64-context pair contractions with the
-backend's own kernels, trains the MLP on the GPU, writes the weights, then
+Measures ``--pairs`` random pair contractions with the backend's own kernels
+in a context of the given ``--precision`` (the one the planner will be used
+with; default the exact-accumulation tensor-core mode), trains the MLP on
+the GPU, writes the weights, then
 for a few circuit workloads executes both the learned planner's choice and the
 flop-count planner's choice and prints their measured times (one JSON line
 per workload).
@@ -56,17 +58,20 @@ def main():
     ap.add_argument("--out", default=str(Path(__file__).resolve().parent / "costmodel_gb300.npz"))
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--budget", type=float, default=600.0, help="seconds allowed for measuring pairs")
+    ap.add_argument("--precision", default="ozaki", choices=["c64", "3xtf32", "6xtf32", "ozaki"])
     args = ap.parse_args()
     import __graft_entry__ as g
 
     pq = g.load_package()
     from pqgb300 import costmodel as CM
 
-    be = pq.GB300Backend(pq.PREC_C64)
+    prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI}
+    be = pq.GB300Backend(prec[args.precision])
     t0 = time.perf_counter()
     model, stats = CM.train_cost_model(be, n_pairs=args.pairs, seed=args.seed, epochs=args.epochs,
                                        budget_s=args.budget, log=lambda d: print(json.dumps(d), flush=True))
     stats["seconds"] = time.perf_counter() - t0
+    stats["precision"] = args.precision
     model.save(args.out, meta={"stats": json.dumps(stats)})
     print(json.dumps({"trained": stats}), flush=True)
 
