@@ -139,7 +139,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="grid6x6_d16_sliced", choices=["grid6x6_d16_sliced", "grid4x5_d12_amps"])
+    ap.add_argument("--workload", default="grid6x6_d16_sliced", choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "pair"],
+                    help="pair: one pairwise contraction of the dominant shape (M x K c64 boundary times K x N "
+                         "c128 gate-column tensor), for kernel profiling")
+    ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
     ap.add_argument("--depth", type=int, default=16)
@@ -158,7 +161,73 @@ def main():
         if rank != 0:
             return 0
         return run_reference(args)
+    if args.workload == "pair":
+        return run_pair(args)
     return run_gb300(args, world, rank)
+
+
+def run_pair(args):
+    """Time one pairwise contraction C[m, n] = sum_k A[m, k] B[k, n] of the
+    6x6 depth-16 plan's dominant shape (a 2^28-element complex64 boundary
+    tensor absorbing a 2^16-element complex128 gate-column tensor: M = 2^20,
+    N = K = 256) through a compiled two-leaf plan, inputs resident; reports
+    the algorithmic rate 8 M N K / time and the error against FP64 on a row
+    sample."""
+    import ctypes as C
+
+    import torch
+
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    from pqgb300 import _lib as L
+
+    M, N, K = (int(x) for x in args.pair.lower().split("x"))
+    prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[args.precision if args.precision != "auto" else "ozaki"]
+    be = pq.GB300Backend(prec)
+    rng = np.random.default_rng(0)
+    A = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))).astype(np.complex64)
+    B = rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))
+    be.save_tensor_data("a", A)
+    be.save_tensor_data("b", B)
+    h = C.c_void_p()
+    L.check(be.lib.pq_plan_create(be.ctx, 2, L.arr(C.c_int32, [2, 2]), L.arr(C.c_int32, [0, 1, 1, 2]), 3,
+                                  L.arr(C.c_int64, [M, K, N]), 1, L.arr(C.c_int32, [0, 1]), 2,
+                                  L.arr(C.c_int32, [0, 2]), C.byref(h)), be.ctx, "plan_create")
+    ids = L.arr(C.c_int64, [be.id_of("a"), be.id_of("b")])
+    out = be.id_of("c")
+    sp = C.c_void_p()
+    be.lib.pq_ctx_stream(be.ctx, C.byref(sp))
+    ext = torch.cuda.ExternalStream(sp.value)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        L.check(be.lib.pq_plan_execute(h, ids, out), be.ctx, "execute")
+    be.sync()
+    times = []
+    n0 = be.launch_count()
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        L.check(be.lib.pq_plan_execute(h, ids, out), be.ctx, "execute")
+        e1.record(ext)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = be.launch_count() - n0
+    got = be.load_tensor_data("c")
+    rows = rng.choice(M, size=min(M, 2048), replace=False)
+    ref = A[rows].astype(np.complex128) @ B
+    err = float(np.max(np.abs(got[rows] - ref)) / np.max(np.abs(ref)))
+    be.lib.pq_plan_destroy(h)
+    be.close()
+    ms = sum(times) / len(times)
+    print(json.dumps({"workload": "pair", "pair": {"M": M, "N": N, "K": K}, "precision": args.precision,
+                      "ms_per_contraction": ms, "algorithmic_tflops": 8.0 * M * N * K / ms / 1e9,
+                      "gpu_launches_per_contraction": launches / max(1, args.steps),
+                      "max_abs_err_over_max_abs_vs_fp64": err, "l2": "flushed between steps (256 MiB write)"}))
+    return 0
 
 
 def run_reference(args):
@@ -448,7 +517,8 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
     if args.workload == "grid6x6_d16_sliced":
         sliced = w["sliced"]
         ms, batched, feats = plan.profile_sliced(sliced, batch=args.batch)
-        roof, kinfo = roofline_from_profile(ms, batched, feats, peaks, peaks_kind, 2 ** len(sliced) // args.batch)
+        roof, kinfo = roofline_from_profile(ms, batched, feats, peaks, peaks_kind, 2 ** len(sliced) // args.batch,
+                                            prec_name)
         extra["kernel_classes"] = kinfo
         # the plain complex-FP64 CUDA path on the same amplitude, and the error
         # of this precision against it
@@ -474,7 +544,7 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
         extra["plan"] = {"planner": w["planner"], "cmacs": w["cmacs"], "max_elems": w["max_elems"]}
         ms = w["plan"].profile()
         feats = w["plan"].features()
-        roof, kinfo = roofline_from_profile(ms, np.zeros(len(ms), bool), feats, peaks, peaks_kind, 1)
+        roof, kinfo = roofline_from_profile(ms, np.zeros(len(ms), bool), feats, peaks, peaks_kind, 1, prec_name)
         extra["kernel_classes"] = kinfo
     cpu_val, cpu_sample_desc = cpu_sample(__import__("__graft_entry__").load_package(), O, args, rows, cols, depth)
     line = {
@@ -492,7 +562,17 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
     return line
 
 
-def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks):
+# Tensor-core operations per algorithmic flop of a complex multiply-add:
+# 3xTF32 issues 3 split products of each of 4 real products, 6xTF32 6; the
+# exact-accumulation scheme 15 slice pairs of 4 real products.
+TENSOR_OPS_PER_FLOP = {"3xtf32": 3.0, "6xtf32": 6.0, "ozaki": 15.0}
+# DRAM bytes of the exact-accumulation GEMM kernel over its algorithmic bytes
+# (|A| + |B| + |C| once), from an ncu capture of the dominant pair at a
+# quarter height (M = 2^18, N = K = 256): 1.032 GB against 1.025 GB.
+OZ_GEMM_TRAFFIC_RATIO = 1.032 / 1.025
+
+
+def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks, prec_name=None):
     """Dominant kernel class by device time; achieved algorithmic FLOP/s or
     bytes/s of that class over its measured launch time."""
     names = {0: "generic", 1: "gemm_simt", 2: "tcgen05", 3: "copy"}
@@ -518,6 +598,17 @@ def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks):
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                 "traffic": None, "kernel": dom, "peak_source": f"{peaks_kind} bf16 sustained",
                 "per_launch_ms": d["ms_per_run"] / d["launches_per_run"]}
+        if dom == "tcgen05" and prec_name in TENSOR_OPS_PER_FLOP:
+            r = TENSOR_OPS_PER_FLOP[prec_name]
+            roof.update({"kernel": "tcgen05 contraction steps (GEMM plus its scale / slice pre-passes)",
+                         "tensor_ops_per_algorithmic_flop": r, "tensor_work_tflops": ach * r,
+                         "tensor_work_frac": ach * r / peak})
+            if prec_name == "ozaki":
+                roof["traffic"] = d["bytes"] / d["launches_per_run"] * OZ_GEMM_TRAFFIC_RATIO
+                roof["traffic_unit"] = "bytes per launch"
+                roof["traffic_source"] = ("k_oz_gemm DRAM bytes per launch: ncu capture of the dominant pair at "
+                                          "M=2^18 (1.007 x algorithmic bytes), scaled to this class's average "
+                                          "algorithmic bytes per launch; the exponent pre-pass reads A once more")
     else:
         ach = d["bytes"] / secs / 1e9
         peak = peaks.get("hbm_gbs")

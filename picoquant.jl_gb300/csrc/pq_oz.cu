@@ -144,12 +144,15 @@ __device__ __forceinline__ int exp_of(double v) {
 }
 
 // Row (side 0: A rows m) or column (side 1: B columns n) scale exponents:
-// e[z * rows + r] = max over k of the frexp exponent of max(|Re|, |Im|).
-// One block per (ROWS-row tile, z); every K offset is staged in shared memory.
+// e[z * rows + r] = frexp exponent of the largest |Re|, |Im| over k.
+// One block per (ROWS-row tile, z); thread t always reads row t % ROWS (K
+// offsets staged in shared memory), keeps a running maximum with four loads
+// in flight, and the 256 / ROWS threads of a row combine at the end.
 template <typename T, int ROWS>
 __global__ void __launch_bounds__(256) k_oz_exp(const T* __restrict__ X, const __grid_constant__ GemmDesc d, int side,
                                                 int64_t rows, int* __restrict__ e_out) {
-  __shared__ int64_t roff[ROWS];
+  static_assert(256 % ROWS == 0, "rows per block");
+  constexpr int KS = 256 / ROWS;  // threads per row
   __shared__ int64_t koff[kMaxK];
   __shared__ int emax[ROWS];
   const int64_t rt = blockIdx.x, z = blockIdx.y;
@@ -158,28 +161,31 @@ __global__ void __launch_bounds__(256) k_oz_exp(const T* __restrict__ X, const _
   const int64_t* rstr = side == 0 ? d.msa : d.nsb;
   const int64_t* kstr = side == 0 ? d.ksa : d.ksb;
   const int64_t* zstr = side == 0 ? d.zsa : d.zsb;
-  for (int t = threadIdx.x; t < ROWS; t += blockDim.x) {
-    const int64_t r = rt * ROWS + t;
-    roff[t] = r < rows ? decode(r, nrm, rdim, rstr) : -1;
-    emax[t] = kExpZero;
-  }
+  for (int t = threadIdx.x; t < ROWS; t += blockDim.x) emax[t] = kExpZero;
   for (int t = threadIdx.x; t < d.K; t += blockDim.x) koff[t] = decode(t, d.nk, d.kdim, kstr);
   __syncthreads();
-  const int64_t zo = decode(z, d.nz, d.zdim, zstr);
   using R = typename Real<T>::R;
-  const int64_t n = (int64_t)ROWS * d.K;
-  for (int64_t o = threadIdx.x; o < n; o += blockDim.x) {
-    const int r = (int)(o % ROWS);
-    const int64_t k = o / ROWS;
-    if (roff[r] < 0) continue;
-    const T v = X[zo + roff[r] + koff[k]];
-    const R m = absmax((R)v.x, (R)v.y);
-    atomicMax(&emax[r], exp_of(m));
+  const int r = threadIdx.x % ROWS, k0 = threadIdx.x / ROWS;
+  const int64_t row = rt * ROWS + r;
+  if (row < rows) {
+    const T* xr = X + decode(z, d.nz, d.zdim, zstr) + decode(row, nrm, rdim, rstr);
+    R mx = 0;
+    int64_t k = k0;
+    for (; k + 3 * KS < d.K; k += 4 * KS) {
+      const T v0 = xr[koff[k]], v1 = xr[koff[k + KS]], v2 = xr[koff[k + 2 * KS]], v3 = xr[koff[k + 3 * KS]];
+      mx = fmax(mx, fmax(fmax(absmax((R)v0.x, (R)v0.y), absmax((R)v1.x, (R)v1.y)),
+                         fmax(absmax((R)v2.x, (R)v2.y), absmax((R)v3.x, (R)v3.y))));
+    }
+    for (; k < d.K; k += KS) {
+      const T v = xr[koff[k]];
+      mx = fmax(mx, absmax((R)v.x, (R)v.y));
+    }
+    atomicMax(&emax[r], exp_of(mx));
   }
   __syncthreads();
   for (int t = threadIdx.x; t < ROWS; t += blockDim.x) {
-    const int64_t r = rt * ROWS + t;
-    if (r < rows) e_out[z * rows + r] = emax[t];
+    const int64_t rr = rt * ROWS + t;
+    if (rr < rows) e_out[z * rows + rr] = emax[t];
   }
 }
 
