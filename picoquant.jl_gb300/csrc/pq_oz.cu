@@ -486,9 +486,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
     using R = typename std::conditional<std::is_same<TC, double2>::value, double, float>::type;
     R* Cr = reinterpret_cast<R*>(C);
+    constexpr int PW = CW >= 16 ? 16 : 8;   // columns per TMEM load
+    constexpr int NU = (CW + 31) / 32;       // columns of the warp's range per lane
     int64_t t = 0;
     for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
       const int64_t nt = tile % ntiles, rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
+      // per-tile offsets and scales, loaded while the tile's MMAs run: the
+      // row's from this lane, the warp's columns spread over the lanes
+      const int64_t m = mt * kRows + r;
+      const bool mrow = m < d.M;
+      const int64_t base = mrow ? decode(z, d.nz, d.zdim, d.zsc) + cm_tab[m] : 0;
+      const int exa = mrow ? ea[z * d.M + m] : kExpZero;
+      const int64_t c0 = nt * TN + h * CW;
+      int ebl[NU];
+      long long cnl[NU];
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int64_t col = c0 + lane + 32 * u;
+        const bool valid = lane + 32 * u < CW && col < d.N;
+        ebl[u] = valid ? eb[z * d.N + col] : kExpZero;
+        cnl[u] = valid ? (long long)cn_tab[col] : 0;
+      }
       bool got = mbar_wait(&sm.accf, (uint32_t)(t & 1));
       got = __all_sync(0xffffffffu, got);  // the TMEM loads below are warp-collective
       if (!got) {
@@ -496,31 +514,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       fence_after();
-      const int64_t m = mt * kRows + r;
-      const bool mrow = m < d.M;
-      const int64_t base = mrow ? decode(z, d.nz, d.zdim, d.zsc) + cm_tab[m] : 0;
-      const int exa = mrow ? ea[z * d.M + m] : kExpZero;
-#pragma unroll 1
-      for (int piece = 0; piece < CW / 8; ++piece) {
+#pragma unroll
+      for (int piece = 0; piece < CW / PW; ++piece) {
         __syncwarp();  // the TMEM loads are warp-collective
-        const uint32_t col = (uint32_t)(h * CW + piece * 8);
-        float l0[8], l1[8], l2[8];
-        tmem_ld8(lane_base + col + 0 * TN, l0);
-        tmem_ld8(lane_base + col + 1 * TN, l1);
-        tmem_ld8(lane_base + col + 2 * TN, l2);
+        const uint32_t col = (uint32_t)(h * CW + piece * PW);
+        float l0[PW], l1[PW], l2[PW];
+        if constexpr (PW == 16) {
+          tmem_ld16(lane_base + col + 0 * TN, l0);
+          tmem_ld16(lane_base + col + 1 * TN, l1);
+          tmem_ld16(lane_base + col + 2 * TN, l2);
+        } else {
+          tmem_ld8(lane_base + col + 0 * TN, l0);
+          tmem_ld8(lane_base + col + 1 * TN, l1);
+          tmem_ld8(lane_base + col + 2 * TN, l2);
+        }
         tmem_wait_ld();
-        if (piece == CW / 8 - 1) {  // every value of this tile is in registers
+        if (piece == CW / PW - 1) {  // every value of this tile is in registers
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&sm.acce);
         }
-        const int64_t n0 = nt * TN + col;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (!mrow || n0 + j >= d.N) break;
-          const int ex = exa + eb[z * d.N + n0 + j];
-          const R v = (exa == kExpZero || ex < -2 * 1100) ? (R)0 : combine(l0[j], l1[j], l2[j], ex, R());
-          Cr[2 * (base + cn_tab[n0 + j]) + part] = v;
+        for (int j = 0; j < PW; ++j) {
+          const int cc = piece * PW + j;  // column within the warp's range
+          const int ebj = __shfl_sync(0xffffffffu, ebl[cc / 32], cc % 32);
+          const long long cnj = __shfl_sync(0xffffffffu, cnl[cc / 32], cc % 32);
+          if (mrow && c0 + cc < d.N) {
+            const int ex = exa + ebj;
+            const R v = (exa == kExpZero || ex < -2 * 1100) ? (R)0 : combine(l0[j], l1[j], l2[j], ex, R());
+            Cr[2 * (base + cnj) + part] = v;
+          }
         }
       }
     }
