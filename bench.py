@@ -139,9 +139,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="grid6x6_d16_sliced", choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "pair"],
-                    help="pair: one pairwise contraction of the dominant shape (M x K c64 boundary times K x N "
-                         "c128 gate-column tensor), for kernel profiling")
+    ap.add_argument("--workload", default="grid6x6_d16_sliced",
+                    choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "grid7x7_d14_learned", "pair"],
+                    help="grid7x7_d14_learned: learned plan selection over sweep orders and 256 seeded greedy "
+                         "orders for a 7x7 depth-14 single amplitude, end to end; pair: one pairwise contraction "
+                         "of the dominant shape (M x K c64 boundary times K x N c128 gate-column tensor), for "
+                         "kernel profiling")
+    ap.add_argument("--candidates", type=int, default=256, help="seeded random-greedy orders ranked by the model")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
@@ -163,7 +167,105 @@ def main():
         return run_reference(args)
     if args.workload == "pair":
         return run_pair(args)
+    if args.workload == "grid7x7_d14_learned":
+        return run_learned(args)
     return run_gb300(args, world, rank)
+
+
+def run_learned(args, rows=7, cols=7, depth=14):
+    """Learned plan selection for a 7x7 depth-14 random circuit (49 qubits),
+    one amplitude: candidate orders (the qubit sweeps, the full-wavefunction
+    order and ``--candidates`` seeded random-greedy draws) ranked by the cost
+    model, the flop-count planner judging; slices chosen for the winner; the
+    end-to-end time from the network to the amplitude (planning included) and
+    the amplitudes of the learned and the flop-count plans and of the plain
+    complex-FP64 path."""
+    import torch
+
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    from pqgb300 import costmodel as CM
+
+    prec_name = args.precision if args.precision != "auto" else "ozaki"
+    prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
+    bits = pq.random_bitstrings(n, 1, seed=2027)[0]
+    target = args.slice_target  # slice only what does not fit 2^target elements
+
+    def network(be):
+        net = pq.build_network(n, gates, decompose=True, backend=be)
+        pq.add_input(net, "0" * n)
+        pq.add_output(net, bits)
+        return net
+
+    def amplitude(plan, sliced):
+        if sliced:
+            return plan.run_sliced(sliced, batch=plan.auto_batch(sliced))
+        plan.execute()
+        return complex(np.asarray(plan.result()).reshape(-1)[0])
+
+    be = pq.GB300Backend(prec)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net = network(be)
+    model = CM.CostModel.load(be)
+    chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=args.candidates)
+    model.close()
+    plan = pq.NetworkPlan(net, steps=chosen["steps"], out_edges=[])
+    sliced = plan.choose_slices(max_sliced=10, log2_target=target)
+    t_plan = time.perf_counter() - t0
+    amp = amplitude(plan, sliced)
+    t_e2e = time.perf_counter() - t0
+    # steady state: the same plan again, inputs resident
+    for _ in range(max(0, args.warmup - 1)):
+        amplitude(plan, sliced)
+    be.sync()
+    ts = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        amplitude(plan, sliced)
+        ts.append(time.perf_counter() - t1)
+    # the flop-count planner's choice, same precision
+    pf = pq.NetworkPlan(net, steps=best_flop["steps"], out_edges=[])
+    sf = pf.choose_slices(max_sliced=10, log2_target=target)
+    t1 = time.perf_counter()
+    amp_f = amplitude(pf, sf)
+    t_flop = time.perf_counter() - t1
+    pf.close()
+    plan.close()
+    be.close()
+    # the plain complex-FP64 path on the flop-count plan
+    be64 = pq.GB300Backend(pq.PREC_C128)
+    net64 = network(be64)
+    p64 = pq.NetworkPlan(net64, steps=best_flop["steps"], out_edges=[])
+    s64 = p64.choose_slices(max_sliced=10, log2_target=target)
+    t1 = time.perf_counter()
+    amp64 = amplitude(p64, s64)
+    t64 = time.perf_counter() - t1
+    p64.close()
+    be64.close()
+    ranked = sorted((c for c in cands if np.isfinite(c.get("pred_us", np.inf))), key=lambda c: c["pred_us"])
+    line = {"workload": f"grid{rows}x{cols}_depth{depth}_learned_plan_single_amplitude", "qubits": n,
+            "depth": depth, "precision": prec_name,
+            "metric": "end-to-end seconds to one amplitude (network -> plan -> amplitude)",
+            "value": t_e2e, "unit": "s", "higher_is_better": False,
+            "planning_s": t_plan, "steady_amplitudes_per_s": len(ts) / sum(ts) if ts else None,
+            "learned_plan": {"name": chosen["name"], "log2_cmacs": float(np.log2(chosen["cmacs"])),
+                             "pred_us": chosen["pred_us"]},
+            "flop_plan": {"name": best_flop["name"], "log2_cmacs": float(np.log2(best_flop["cmacs"])),
+                          "seconds": t_flop},
+            "candidates": len(cands), "candidates_within_flop_judge": len(ranked),
+            "model_ranking_top5": [(c["name"], c["pred_us"]) for c in ranked[:5]],
+            "sliced_bonds": len(sliced), "slice_target_log2": target,
+            "amplitude": [amp.real, amp.imag],
+            "rel_diff_learned_vs_flop_plan": abs(amp - amp_f) / abs(amp_f),
+            "rel_err_vs_fp64": abs(amp - amp64) / abs(amp64), "plain_fp64_seconds": t64,
+            "data": "synthetic (seeded random circuit)"}
+    print(json.dumps(line))
+    return 0
 
 
 def run_pair(args):

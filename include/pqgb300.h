@@ -55,8 +55,10 @@ extern "C" {
  *                  TF32 hi+lo parts (3 products: hh, hl, lh), FP32 TMEM
  *                  accumulation over 8-deep K chunks folded into
  *                  Kahan-compensated FP32 sums.
- * PQ_PREC_3XBF16 : accepted; runs as PQ_PREC_C64 (no bf16 tensor-core class:
- *                  a bf16 hi/lo split cannot reach 1e-6 amplitude error).
+ * PQ_PREC_3XBF16 : as PQ_PREC_OZAKI with three bf16 slices (6 slice-pair
+ *                  products, about 21 significant bits: pair error ~1e-6, not
+ *                  enough for 1e-6 amplitude error); K > 512 runs as
+ *                  PQ_PREC_3XTF32.
  * PQ_PREC_6XTF32 : as PQ_PREC_3XTF32 with a hi+mid+lo TF32 split and 6
  *                  products (hh, hm, mh, hl, lh, mm) per real product.
  * PQ_PREC_OZAKI  : as PQ_PREC_C64, but large GEMM-shaped contractions with

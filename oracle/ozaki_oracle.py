@@ -24,7 +24,15 @@ import numpy as np
 
 N_SLICES = 5
 BITS = 7
-PAIRS = [(i, j) for lvl in range(N_SLICES) for i in range(lvl + 1) for j in [lvl - i]]
+
+
+def pairs(n_slices=N_SLICES):
+    """Slice pairs (i, j) with i + j < n_slices (15 for five slices, 6 for
+    the three of PQ_PREC_3XBF16)."""
+    return [(i, lvl - i) for lvl in range(n_slices) for i in range(lvl + 1)]
+
+
+PAIRS = pairs()
 ZERO_EXP = -4096
 
 
@@ -37,11 +45,11 @@ def row_exponents(X):
     return e
 
 
-def slices(x):
+def slices(x, n_slices=N_SLICES):
     """The fixed-grid slices of x (|x| < 1), each exact in bf16."""
     out = []
     r = np.array(x, dtype=np.float64)
-    for i in range(N_SLICES):
+    for i in range(n_slices):
         g = 2.0 ** (BITS * (i + 1))
         s = np.rint(r * g) / g
         out.append(s)
@@ -56,7 +64,7 @@ def bf16_exact(v):
     return np.all(np.rint(m * 256) == m * 256)
 
 
-def ozaki_matmul(A, B, out_dtype=np.complex64):
+def ozaki_matmul(A, B, out_dtype=np.complex64, n_slices=N_SLICES):
     """C = A @ B (A: M x K, B: K x N complex) the way the device computes it;
     returns (C rounded to out_dtype, levels (L0, L1, L2) complex, unscaled)."""
     ea = row_exponents(A)
@@ -65,10 +73,10 @@ def ozaki_matmul(A, B, out_dtype=np.complex64):
     sb = np.where(eb == ZERO_EXP, 0, -eb).astype(np.float64)
     As = A * np.exp2(sa)[:, None]
     Bs = B * np.exp2(sb)[None, :]
-    ar, ai = slices(As.real), slices(As.imag)
-    br, bi = slices(Bs.real), slices(Bs.imag)
+    ar, ai = slices(As.real, n_slices), slices(As.imag, n_slices)
+    br, bi = slices(Bs.real, n_slices), slices(Bs.imag, n_slices)
     lv = [np.zeros((A.shape[0], B.shape[1]), dtype=np.complex128) for _ in range(3)]
-    for i, j in PAIRS:
+    for i, j in pairs(n_slices):
         lvl = min(i + j, 2)
         lv[lvl] += (ar[i] @ br[j] - ai[i] @ bi[j]) + 1j * (ar[i] @ bi[j] + ai[i] @ br[j])
     scale = np.exp2((ea[:, None] + eb[None, :]).astype(np.float64))
@@ -77,15 +85,16 @@ def ozaki_matmul(A, B, out_dtype=np.complex64):
     return C.astype(out_dtype), lv
 
 
-def error_bound(A, B, ref):
+def error_bound(A, B, ref, n_slices=N_SLICES):
     """Per-element bound on |device result - A @ B| (A: M x K, B: K x N):
     the output rounding (2^-24 relative per component, |.| <= 2^-23 |ref|)
-    plus, per real product, the dropped slice pairs of level >= 5 and the
-    slice residuals (below 2^-34 of the row / column scales 2^ea, 2^eb), two
+    plus, per real product, the dropped slice pairs of level >= n_slices and
+    the slice residuals (below 2^-(7 n_slices - 1) of the row / column scales
+    2^ea, 2^eb, with a factor 2 of margin), two
     real products per component and K terms, and the truncations of the small
     level-2-4 accumulator (below 2^-30 of the scales after K terms)."""
     ea = row_exponents(A).astype(np.float64)
     eb = row_exponents(B.T).astype(np.float64)
     K = A.shape[1]
     scale = np.exp2(np.minimum(ea, 4096)[:, None] + np.minimum(eb, 4096)[None, :])
-    return 2.0 ** -23 * np.abs(ref) + (2.0 ** -32 * K + 2.0 ** -29) * scale
+    return 2.0 ** -23 * np.abs(ref) + (2.0 ** -(7 * n_slices - 3) * K + 2.0 ** -29) * scale

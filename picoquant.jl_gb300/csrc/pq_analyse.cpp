@@ -239,7 +239,9 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
   const bool narrow = std::min(G.M, G.N) >= 8 && std::max(G.M, G.N) >= 256;
   bool gemm_shape = k_both && G.K >= 16 && ((G.M >= 32 && G.N >= 32) || narrow) &&
                     (double)G.M * (double)G.N * (double)G.K * (double)G.Z >= double(1 << 20);
-  if (gemm_shape && (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32 || precision == PQ_PREC_OZAKI) &&
+  if (gemm_shape &&
+      (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32 || precision == PQ_PREC_OZAKI ||
+       precision == PQ_PREC_3XBF16) &&
       tc_eligible(precision, G))
     out.kclass = KC_TC;
   else if (gemm_shape || (k_both && out.ksize > kGenericKTab && G.M >= 8 && G.N >= 8))

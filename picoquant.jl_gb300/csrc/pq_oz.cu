@@ -81,9 +81,6 @@ namespace {
 using namespace tcg;
 
 constexpr int TK = 16;
-constexpr int kSlices = 5;                       // bf16 slices per real value
-constexpr int kPlanes = 2 * kSlices;             // per operand: Re s0..s4, Im s0..s4
-constexpr int kPairs = 15;                       // slice pairs (i, j) with i + j <= 4
 constexpr int kThreads = 576;                    // producer, MMA, 8 converter + 8 epilogue warps
 constexpr int kConvWarps = 8, kEpiWarps = 8;
 constexpr int kRows = 64;                        // complex rows of A per tile
@@ -92,24 +89,42 @@ constexpr int kExpZero = -4096;                  // exponent of an all-zero row
 constexpr int64_t kMaxK = 512;                   // exact level-0/1 sums up to this K
 
 // Tile width N: 128 for general pairs, 64 / 32 / 16 for narrow ones.
-template <int TN>
+// Slices per real value: 5 for PQ_PREC_OZAKI (15 slice pairs, i + j <= 4),
+// 3 for PQ_PREC_3XBF16 (6 pairs, i + j <= 2).
+template <int NSL>
+struct Sl {
+  static_assert(NSL == 5 || NSL == 3, "slice count");
+  static constexpr int planes = 2 * NSL;  // per operand: Re s0.., Im s0..
+  static constexpr int pairs = NSL == 5 ? 15 : 6;
+};
+
+template <int TN, int NSL>
 struct OzCfg {
   static constexpr int kBTile = TN * TK;                                   // bf16 per B plane tile
-  static constexpr uint32_t b_bytes = kPlanes * kBTile * 2;                // B planes of one K tile
-  static constexpr uint32_t stage_bytes = kSlices * kStackBytes + b_bytes;
-  static constexpr int stages = TN == 128 ? 3 : 4;
+  static constexpr uint32_t b_bytes = Sl<NSL>::planes * kBTile * 2;        // B planes of one K tile
+  static constexpr uint32_t stage_bytes = NSL * kStackBytes + b_bytes;
+  static constexpr int stages = (TN == 128 && NSL == 5) ? 3 : 4;
   static constexpr uint32_t tmem_cols = TN == 128 ? 512 : (TN == 64 ? 256 : (TN == 32 ? 128 : 64));
   static constexpr int cw = TN / 2;                                         // columns per epilogue warp
   static_assert(3 * TN <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
 };
 
-// slice pairs, level 0 first, then level 1, then levels 4, 3, 2 (the inexact
-// accumulator takes its small terms first)
+// slice pairs, level 0 first, then level 1, then the higher levels (the
+// inexact accumulator takes its small terms first).  Five slices:
 //   i: 0 0 1 0 1 2 3 4 0 1 2 3 0 1 2
 //   j: 0 1 0 4 3 2 1 0 3 2 1 0 2 1 0
+// three slices:
+//   i: 0 0 1 0 1 2
+//   j: 0 1 0 2 1 0
 // (4-bit fields, pair p in bits [4p, 4p + 4))
-__host__ __device__ constexpr int pair_i(int p) { return (int)((uint64_t)0x210321043210100ull >> (4 * p)) & 15; }
-__host__ __device__ constexpr int pair_j(int p) { return (int)((uint64_t)0x12012301234010ull >> (4 * p)) & 15; }
+template <int NSL>
+__host__ __device__ constexpr int pair_i(int p) {
+  return (int)((NSL == 5 ? 0x210321043210100ull : 0x210100ull) >> (4 * p)) & 15;
+}
+template <int NSL>
+__host__ __device__ constexpr int pair_j(int p) {
+  return (int)((NSL == 5 ? 0x12012301234010ull : 0x12010ull) >> (4 * p)) & 15;
+}
 
 __host__ __device__ constexpr int level_of(int p) { return p == 0 ? 0 : (p < 3 ? 1 : 2); }
 __host__ __device__ constexpr bool first_of_level(int p) { return p == 0 || p == 1 || p == 3; }
@@ -190,12 +205,12 @@ __global__ void __launch_bounds__(256) k_oz_exp(const T* __restrict__ X, const _
 }
 
 // The slices of x (|x| < 1 after scaling); every step is exact in R.
-template <typename R>
+template <typename R, int NSL>
 __device__ __forceinline__ void slices(R x, float* s) {
   R r = x;
   R g = (R)128.0, gi = (R)(1.0 / 128.0);  // 2^7(i+1) and its inverse (exact)
 #pragma unroll
-  for (int i = 0; i < kSlices; ++i) {
+  for (int i = 0; i < NSL; ++i) {
     const R si = round_int(r * g) * gi;
     s[i] = (float)si;
     r -= si;
@@ -217,7 +232,7 @@ __device__ __forceinline__ float2 inv_scale(int e) {
 __device__ __forceinline__ float scale_row(float x, int, float2 f) { return (x * f.x) * f.y; }
 __device__ __forceinline__ double scale_row(double x, int e, float2) { return ldexp(x, -e); }
 
-template <typename T, int ROWS>
+template <typename T, int ROWS, int NSL>
 __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_bfloat16* __restrict__ planes,
                                                  const __grid_constant__ GemmDesc d, int side, int64_t rows,
                                                  int64_t rtiles, int64_t ktiles, const int* __restrict__ e_in) {
@@ -244,34 +259,34 @@ __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_b
   __syncthreads();
   const int64_t zo = decode(z, d.nz, d.zdim, zstr);
   using R = typename Real<T>::R;
-  __nv_bfloat16* tile = planes + (((z * rtiles + rt) * ktiles + kt) * kPlanes) * (int64_t)TILE;
+  __nv_bfloat16* tile = planes + (((z * rtiles + rt) * ktiles + kt) * Sl<NSL>::planes) * (int64_t)TILE;
   for (int o = threadIdx.x; o < TILE; o += blockDim.x) {
     // o = ((kc * GROUPS + g) * 8 + r8) * 8 + k8: core matrix (kc, g), row r8, K k8
     const int core = o >> 6, within = o & 63;
     const int kc = core / GROUPS, g = core - kc * GROUPS;
     const int r = g * 8 + (within >> 3), k = kc * 8 + (within & 7);
-    float re[kSlices], im[kSlices];
+    float re[NSL], im[NSL];
 #pragma unroll
-    for (int i = 0; i < kSlices; ++i) re[i] = im[i] = 0.f;
+    for (int i = 0; i < NSL; ++i) re[i] = im[i] = 0.f;
     if (roff[r] >= 0 && koff[k] >= 0 && rexp[r] != kExpZero) {
       const T v = X[zo + roff[r] + koff[k]];
-      slices<R>(scale2((R)v.x, -rexp[r]), re);
-      slices<R>(scale2((R)v.y, -rexp[r]), im);
+      slices<R, NSL>(scale2((R)v.x, -rexp[r]), re);
+      slices<R, NSL>(scale2((R)v.y, -rexp[r]), im);
     }
 #pragma unroll
-    for (int i = 0; i < kSlices; ++i) {
-      tile[(0 * kSlices + i) * TILE + o] = __float2bfloat16_rn(re[i]);
-      tile[(1 * kSlices + i) * TILE + o] = __float2bfloat16_rn(im[i]);
+    for (int i = 0; i < NSL; ++i) {
+      tile[(0 * NSL + i) * TILE + o] = __float2bfloat16_rn(re[i]);
+      tile[(1 * NSL + i) * TILE + o] = __float2bfloat16_rn(im[i]);
     }
   }
 }
 
-template <int TN>
+template <int TN, int NSL>
 struct alignas(1024) OzSmem {
-  unsigned char stage[OzCfg<TN>::stages][OzCfg<TN>::stage_bytes];  // A stacks, then B planes
-  int64_t koff[kMaxK];                                              // A's K offsets
-  uint64_t full[OzCfg<TN>::stages];
-  uint64_t empty[OzCfg<TN>::stages];
+  unsigned char stage[OzCfg<TN, NSL>::stages][OzCfg<TN, NSL>::stage_bytes];  // A stacks, then B planes
+  int64_t koff[kMaxK];                                                        // A's K offsets
+  uint64_t full[OzCfg<TN, NSL>::stages];
+  uint64_t empty[OzCfg<TN, NSL>::stages];
   uint64_t accf;
   uint64_t acce;
   uint64_t drain;
@@ -304,17 +319,18 @@ __device__ __forceinline__ void sts64(uint32_t addr, uint32_t a, uint32_t b) {
 // Generic-proxy shared-memory writes made visible to the tensor core's reads.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-template <typename TA, typename TC, int TN>
+template <typename TA, typename TC, int TN, int NSL>
 __global__ void __launch_bounds__(kThreads, 1)
     k_oz_gemm(const TA* __restrict__ A, const __nv_bfloat16* __restrict__ pb, TC* __restrict__ C,
               const __grid_constant__ GemmDesc d, const int64_t* __restrict__ cm_tab,
               const int64_t* __restrict__ cn_tab, const int* __restrict__ ea, const int* __restrict__ eb,
               int64_t mtiles, int64_t ntiles, int64_t ktiles, int* status) {
-  using CF = OzCfg<TN>;
+  using CF = OzCfg<TN, NSL>;
+  constexpr int kSlices = NSL, kPlanes = Sl<NSL>::planes, kPairs = Sl<NSL>::pairs;
   constexpr int kStages = CF::stages;
   constexpr uint32_t kTmemCols = CF::tmem_cols;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  OzSmem<TN>& sm = *reinterpret_cast<OzSmem<TN>*>(smem_raw);
+  OzSmem<TN, NSL>& sm = *reinterpret_cast<OzSmem<TN, NSL>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ntot = ntiles * mtiles * d.Z;
 
@@ -385,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint64_t b0 = smem_desc(sa + kSlices * kStackBytes, BLBO, SBO);
 #pragma unroll
           for (int p = 0; p < kPairs; ++p) {
-            const int i = pair_i(p), j = pair_j(p);
+            const int i = pair_i<NSL>(p), j = pair_j<NSL>(p);
             const uint32_t acc = (kt == 0 && first_of_level(p)) ? 0u : 1u;
             const uint32_t dl = tmem + (uint32_t)(level_of(p) * TN);
             const uint64_t x1 = a0 + (uint64_t)((i * kStackBytes) >> 4);             // [Ar; Ai]
@@ -447,8 +463,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float a[kSlices], b[kSlices];
-          slices<R>(scale_row((R)cur[q].x, e, f), a);
-          slices<R>(scale_row((R)cur[q].y, e, f), b);
+          slices<R, NSL>(scale_row((R)cur[q].x, e, f), a);
+          slices<R, NSL>(scale_row((R)cur[q].y, e, f), b);
 #pragma unroll
           for (int i = 0; i < kSlices; ++i) {
             re[i][q] = a[i];
@@ -565,7 +581,7 @@ struct OzLayout {
   size_t pb, cm, cn, ea, eb, total;  // byte offsets from the aligned base
 };
 
-OzLayout layout(const GemmDesc& d) {
+OzLayout layout(const GemmDesc& d, int nsl) {
   OzLayout L;
   L.tn = oz_tile_n(d.N);
   L.mt = ceil_div(d.M, kRows);
@@ -573,7 +589,7 @@ OzLayout layout(const GemmDesc& d) {
   L.kt = ceil_div(d.K, TK);
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   L.pb = 0;
-  L.cm = up(L.pb + (size_t)(d.Z * L.nt * L.kt) * kPlanes * (L.tn * TK) * 2);
+  L.cm = up(L.pb + (size_t)(d.Z * L.nt * L.kt) * (2 * nsl) * (L.tn * TK) * 2);
   L.cn = up(L.cm + (size_t)d.M * 8);
   L.ea = up(L.cn + (size_t)d.N * 8);
   L.eb = up(L.ea + (size_t)(d.Z * d.M) * 4);
@@ -605,77 +621,68 @@ GemmDesc swapped(const GemmDesc& d) {
 }
 bool needs_swap(const GemmDesc& d) { return d.M < 64 && d.N > d.M; }
 
-template <typename T, int ROWS>
+template <typename T, int ROWS, int NSL>
 void prep_b(const void* X, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
             cudaStream_t s) {
   k_oz_exp<T, ROWS><<<dim3((unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, d, 1, d.N, e);
-  k_oz_pack<T, ROWS><<<dim3((unsigned)kt, (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, planes, d, 1,
+  k_oz_pack<T, ROWS, NSL><<<dim3((unsigned)kt, (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, planes, d, 1,
                                                                                        d.N, rtiles, kt, e);
 }
 
-template <typename T>
+template <typename T, int NSL>
 void prep_b_tn(const void* X, int tn, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
                cudaStream_t s) {
-  if (tn == 128) prep_b<T, 128>(X, planes, e, d, rtiles, kt, s);
-  else if (tn == 64) prep_b<T, 64>(X, planes, e, d, rtiles, kt, s);
-  else if (tn == 32) prep_b<T, 32>(X, planes, e, d, rtiles, kt, s);
-  else prep_b<T, 16>(X, planes, e, d, rtiles, kt, s);
+  if (tn == 128) prep_b<T, 128, NSL>(X, planes, e, d, rtiles, kt, s);
+  else if (tn == 64) prep_b<T, 64, NSL>(X, planes, e, d, rtiles, kt, s);
+  else if (tn == 32) prep_b<T, 32, NSL>(X, planes, e, d, rtiles, kt, s);
+  else prep_b<T, 16, NSL>(X, planes, e, d, rtiles, kt, s);
 }
 
-template <typename TA, typename TC, int TN>
+template <typename TA, typename TC, int TN, int NSL>
 cudaError_t oz_gemm_launch(const void* A, const __nv_bfloat16* pb, void* C, const GemmDesc& d, const int64_t* cm,
                            const int64_t* cn, const int* ea, const int* eb, const OzLayout& L, int* status,
                            cudaStream_t s) {
-  static_assert(sizeof(OzSmem<TN>) + 1024 <= 232448, "shared memory layout exceeds 227 KiB");
-  const size_t smem = sizeof(OzSmem<TN>) + 1024;
+  static_assert(sizeof(OzSmem<TN, NSL>) + 1024 <= 232448, "shared memory layout exceeds 227 KiB");
+  const size_t smem = sizeof(OzSmem<TN, NSL>) + 1024;
   static bool attr = false;
   if (!attr) {
     cudaError_t e =
-        cudaFuncSetAttribute(k_oz_gemm<TA, TC, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_oz_gemm<TA, TC, TN, NSL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   const int64_t tiles = L.mt * L.nt * d.Z;
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
-  k_oz_gemm<TA, TC, TN><<<grid, kThreads, smem, s>>>((const TA*)A, pb, (TC*)C, d, cm, cn, ea, eb, L.mt, L.nt, L.kt,
+  k_oz_gemm<TA, TC, TN, NSL><<<grid, kThreads, smem, s>>>((const TA*)A, pb, (TC*)C, d, cm, cn, ea, eb, L.mt, L.nt, L.kt,
                                                      status);
   return cudaGetLastError();
 }
 
-template <typename TA, typename TC>
+template <typename TA, typename TC, int NSL>
 cudaError_t oz_gemm_tn(const void* A, const __nv_bfloat16* pb, void* C, const GemmDesc& d, const int64_t* cm,
                        const int64_t* cn, const int* ea, const int* eb, const OzLayout& L, int* status,
                        cudaStream_t s) {
-  if (L.tn == 128) return oz_gemm_launch<TA, TC, 128>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
-  if (L.tn == 64) return oz_gemm_launch<TA, TC, 64>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
-  if (L.tn == 32) return oz_gemm_launch<TA, TC, 32>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
-  return oz_gemm_launch<TA, TC, 16>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  if (L.tn == 128) return oz_gemm_launch<TA, TC, 128, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  if (L.tn == 64) return oz_gemm_launch<TA, TC, 64, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  if (L.tn == 32) return oz_gemm_launch<TA, TC, 32, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
+  return oz_gemm_launch<TA, TC, 16, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, s);
 }
 
 bool eligible_oriented(const GemmDesc& d) {
   if (d.M < 64 || d.N < 8 || d.K < 16 || d.K > kMaxK) return false;
   if (d.Z > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535 || ceil_div(d.M, 128) > 65535) return false;
-  return layout(d).total <= (size_t(24) << 30);
+  return layout(d, 5).total <= (size_t(24) << 30);
 }
 
 }  // namespace
 
 bool oz_eligible(const GemmDesc& d) { return eligible_oriented(needs_swap(d) ? swapped(d) : d); }
 
-size_t oz_scratch_bytes(const GemmDesc& d) { return layout(needs_swap(d) ? swapped(d) : d).total; }
+size_t oz_scratch_bytes(int slices, const GemmDesc& d) { return layout(needs_swap(d) ? swapped(d) : d, slices).total; }
 
-cudaError_t launch_oz(int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d0, void* scratch,
-                      size_t scratch_bytes, int* status, cudaStream_t stream) {
-  if (!oz_eligible(d0)) return cudaErrorNotSupported;
-  const bool swap = needs_swap(d0);
-  const GemmDesc d = swap ? swapped(d0) : d0;
-  if (swap) {
-    std::swap(A, B);
-    std::swap(ta, tb);
-  }
-  const OzLayout L = layout(d);
-  if (!scratch || scratch_bytes < L.total) return cudaErrorInvalidValue;
-  char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+template <int NSL>
+static cudaError_t launch_oz_n(int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
+                               char* base, const OzLayout& L, int* status, cudaStream_t stream) {
   auto* pb = (__nv_bfloat16*)(base + L.pb);
   auto* cm = (int64_t*)(base + L.cm);
   auto* cn = (int64_t*)(base + L.cn);
@@ -688,18 +695,34 @@ cudaError_t launch_oz(int ta, int tb, int tc, const void* A, const void* B, void
     k_oz_exp<float2, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, stream>>>(
         (const float2*)A, d, 0, d.M, ea);
   if (tb == PQ_C128)
-    prep_b_tn<double2>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
+    prep_b_tn<double2, NSL>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
   else
-    prep_b_tn<float2>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
+    prep_b_tn<float2, NSL>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
   const int64_t idx_blocks = std::min<int64_t>(ceil_div(d.M + d.N, 256), 152 * 8);
   k_result_index<<<(unsigned)idx_blocks, 256, 0, stream>>>(d, cm, cn);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (ta == PQ_C128)
-    return tc == PQ_C128 ? oz_gemm_tn<double2, double2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
-                         : oz_gemm_tn<double2, float2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
-  return tc == PQ_C128 ? oz_gemm_tn<float2, double2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
-                       : oz_gemm_tn<float2, float2>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
+    return tc == PQ_C128 ? oz_gemm_tn<double2, double2, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
+                         : oz_gemm_tn<double2, float2, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
+  return tc == PQ_C128 ? oz_gemm_tn<float2, double2, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, stream)
+                       : oz_gemm_tn<float2, float2, NSL>(A, pb, C, d, cm, cn, ea, eb, L, status, stream);
+}
+
+cudaError_t launch_oz(int slices, int ta, int tb, int tc, const void* A, const void* B, void* C,
+                      const GemmDesc& d0, void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream) {
+  if (!oz_eligible(d0) || (slices != 5 && slices != 3)) return cudaErrorNotSupported;
+  const bool swap = needs_swap(d0);
+  const GemmDesc d = swap ? swapped(d0) : d0;
+  if (swap) {
+    std::swap(A, B);
+    std::swap(ta, tb);
+  }
+  const OzLayout L = layout(d, slices);
+  if (!scratch || scratch_bytes < L.total) return cudaErrorInvalidValue;
+  char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  return slices == 5 ? launch_oz_n<5>(ta, tb, tc, A, B, C, d, base, L, status, stream)
+                     : launch_oz_n<3>(ta, tb, tc, A, B, C, d, base, L, status, stream);
 }
 
 }  // namespace pq

@@ -369,39 +369,44 @@ cudaError_t gemm_launch(const float* pa, const float* pb, void* C, const GemmDes
 
 }  // namespace
 
-// PQ_PREC_OZAKI runs the exact-accumulation kernels (pq_oz.cu) where their
-// limits allow (K <= 512) and the 6xTF32 kernels otherwise.
+// PQ_PREC_OZAKI / PQ_PREC_3XBF16 run the exact-accumulation kernels
+// (pq_oz.cu, 5 / 3 bf16 slices) where their limits allow (K <= 512) and the
+// 6xTF32 / 3xTF32 kernels otherwise.
 static bool tf32_eligible(const GemmDesc& d) {
   if (d.M < 64 || d.N < 64 || d.K < 16) return false;
   return d.Z <= 65535 && ceil_div(d.N, TN) <= 65535 && ceil_div(d.M, TM) <= 65535;
 }
-static int tf32_precision(int precision) { return precision == PQ_PREC_OZAKI ? PQ_PREC_6XTF32 : precision; }
+static int tf32_precision(int precision) {
+  return precision == PQ_PREC_OZAKI ? PQ_PREC_6XTF32 : (precision == PQ_PREC_3XBF16 ? PQ_PREC_3XTF32 : precision);
+}
+static bool sliced_bf16(int precision) { return precision == PQ_PREC_OZAKI || precision == PQ_PREC_3XBF16; }
+static int bf16_slices(int precision) { return precision == PQ_PREC_OZAKI ? 5 : 3; }
 
 size_t tc_scratch_bytes(int precision, const GemmDesc& d) {
-  if (precision == PQ_PREC_OZAKI && oz_eligible(d)) return oz_scratch_bytes(d);
+  if (sliced_bf16(precision) && oz_eligible(d)) return oz_scratch_bytes(bf16_slices(precision), d);
   const int P = 2 * splits_of(tf32_precision(precision));
   const int64_t mt = ceil_div(d.M, TM), nt = ceil_div(d.N, TN), kt = ceil_div(d.K, TK);
   return (size_t)(d.Z * (mt * kATile + nt * kBTile) * kt * P * 4) + (size_t)(d.M + d.N) * 8 + 1024;
 }
 
 bool tc_eligible(int precision, const GemmDesc& d) {
-  if (precision != PQ_PREC_3XTF32 && precision != PQ_PREC_6XTF32 && precision != PQ_PREC_OZAKI) return false;
-  if (precision == PQ_PREC_OZAKI && oz_eligible(d)) return true;
+  if (precision != PQ_PREC_3XTF32 && precision != PQ_PREC_6XTF32 && !sliced_bf16(precision)) return false;
+  if (sliced_bf16(precision) && oz_eligible(d)) return true;
   return tf32_eligible(d) && tc_scratch_bytes(precision, d) <= (size_t(24) << 30);
 }
 
 int tc_launch_count(int precision, const GemmDesc& d) {
   // exponents of A and B, slices of B, result index table, GEMM (A is sliced
   // inside it); or the TF32 path's index table, two packs, GEMM
-  return (precision == PQ_PREC_OZAKI && oz_eligible(d)) ? 5 : 4;
+  return (sliced_bf16(precision) && oz_eligible(d)) ? 5 : 4;
 }
 
 cudaError_t launch_tc(int precision, int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
                       void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream) {
   if (!tc_eligible(precision, d)) return cudaErrorNotSupported;
   if (!scratch || scratch_bytes < tc_scratch_bytes(precision, d)) return cudaErrorInvalidValue;
-  if (precision == PQ_PREC_OZAKI && oz_eligible(d))
-    return launch_oz(ta, tb, tc, A, B, C, d, scratch, scratch_bytes, status, stream);
+  if (sliced_bf16(precision) && oz_eligible(d))
+    return launch_oz(bf16_slices(precision), ta, tb, tc, A, B, C, d, scratch, scratch_bytes, status, stream);
   const int NS = splits_of(tf32_precision(precision));
   const int64_t mt = ceil_div(d.M, TM), nt = ceil_div(d.N, TN), kt = ceil_div(d.K, TK);
   float* pa = (float*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);

@@ -15,7 +15,7 @@ OZ_LAUNCHES = 5  # exponents of A and B, slices of B, result index table, GEMM
 
 
 def launches_for(be, k):
-    return OZ_LAUNCHES if be.precision == 5 and k <= 512 else TC_LAUNCHES
+    return OZ_LAUNCHES if be.precision in (3, 5) and k <= 512 else TC_LAUNCHES
 
 
 def rel_err(a, b):
@@ -28,8 +28,8 @@ def rand(rng, dims):
     return rng.standard_normal(dims) + 1j * rng.standard_normal(dims)
 
 
-@pytest.fixture(params=[(2, None), (2, 0), (4, None), (5, None), (5, 0)],
-                ids=["3xtf32-mixed", "3xtf32-c64all", "6xtf32-mixed", "ozaki-mixed", "ozaki-c64all"])
+@pytest.fixture(params=[(2, None), (2, 0), (4, None), (5, None), (5, 0), (3, None)],
+                ids=["3xtf32-mixed", "3xtf32-c64all", "6xtf32-mixed", "ozaki-mixed", "ozaki-c64all", "3xbf16-mixed"])
 def be(request, pq):
     prec, small = request.param
     b = pq.GB300Backend(prec, small_elems=small)
@@ -143,7 +143,7 @@ def test_batched_hyper_mode_via_plan(pq, O, be):
     be.lib.pq_plan_destroy(h)
 
 
-@pytest.mark.parametrize("prec", [2, 4, 5], ids=["3xtf32", "6xtf32", "ozaki"])
+@pytest.mark.parametrize("prec", [2, 4, 5, 3], ids=["3xtf32", "6xtf32", "ozaki", "3xbf16"])
 def test_tc_plan_amplitude(pq, O, prec):
     """A sliced single amplitude on the tensor-core path vs the state vector."""
     be = pq.GB300Backend(prec)
@@ -158,7 +158,8 @@ def test_tc_plan_amplitude(pq, O, prec):
     sliced = plan.choose_slices(max_sliced=4, log2_target=28)
     amp = plan.run_sliced(sliced, batch=16)
     ref = O.statevector(16, g)[O.amplitude_index(bits)]
-    assert abs(amp - ref) / 2.0 ** -8 < 1e-6
+    # three bf16 slices keep about 21 bits: a looser bound for that mode
+    assert abs(amp - ref) / 2.0 ** -8 < (2e-5 if prec == 3 else 1e-6)
     plan.close()
     be.close()
 
@@ -237,6 +238,25 @@ def test_ozaki_narrow_pairs(pq, m, n, k):
     A, B = A.astype(np.complex128), B.astype(np.complex128)
     ref = A @ B
     assert np.all(np.abs(got - ref) <= ozaki_bound(A, B, ref))
+
+
+def test_3xbf16_matches_cpu_restatement(pq):
+    """Three bf16 slices: the device result is the CPU restatement with
+    n_slices = 3 up to one final rounding, within the scheme's bound."""
+    from oracle import ozaki_oracle as Z
+
+    rng = np.random.default_rng(10)
+    A = rand(rng, (384, 128)).astype(np.complex64)
+    B = rand(rng, (128, 200)).astype(np.complex64)
+    be = pq.GB300Backend(3, small_elems=0)
+    got, nl = run(be, A, [-1, 1], B, [1, -2])
+    be.close()
+    assert nl == OZ_LAUNCHES
+    A, B = A.astype(np.complex128), B.astype(np.complex128)
+    orc, _ = Z.ozaki_matmul(A, B, n_slices=3)
+    ref = A @ B
+    assert np.all(np.abs(got - ref) <= Z.error_bound(A, B, ref, n_slices=3))
+    assert np.max(np.abs(got - orc)) <= 2.0 ** -22 * np.max(np.abs(orc))
 
 
 def test_ozaki_k512_exact_limit(pq):
