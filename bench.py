@@ -140,12 +140,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="grid6x6_d16_sliced",
-                    choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "grid7x7_d14_learned", "pair"],
+                    choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "grid7x7_d14_learned", "uneven512", "pair"],
                     help="grid7x7_d14_learned: learned plan selection over sweep orders and 256 seeded greedy "
                          "orders for a 7x7 depth-14 single amplitude, end to end; pair: one pairwise contraction "
                          "of the dominant shape (M x K c64 boundary times K x N c128 gate-column tensor), for "
                          "kernel profiling")
     ap.add_argument("--candidates", type=int, default=256, help="seeded random-greedy orders ranked by the model")
+    ap.add_argument("--circuits", type=int, default=512, help="circuits of the uneven512 workload")
+    ap.add_argument("--check", type=int, default=8, help="uneven512 circuits also run in complex128 for the error")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
@@ -169,7 +171,145 @@ def main():
         return run_pair(args)
     if args.workload == "grid7x7_d14_learned":
         return run_learned(args)
+    if args.workload == "uneven512":
+        return run_uneven(args)
     return run_gb300(args, world, rank)
+
+
+AMP_INDEX = "__amplitudes__"
+
+
+def batched_outputs(pq, net, bitstrings):
+    """Output tensors for a batch of bitstrings: qubit q's output becomes a
+    2 x B matrix whose column b is the basis vector of bitstring b's bit, and
+    all of them share one extra index, so a single contraction leaves the B
+    amplitudes as a vector over that index (a hyper index of the plan)."""
+    from pqgb300 import network as NW
+
+    B = len(bitstrings)
+    for i in range(net.number_qubits):
+        pos = net.qubit_ordering[i]
+        index = net.output_qubits[pos - 1]
+        data = np.zeros((2, B), dtype=np.complex128)
+        for b, s in enumerate(bitstrings):
+            data[1 if s[i] == "1" else 0, b] = 1.0
+        label = NW.new_label(net, "node")
+        net.nodes[label] = NW.Node([index, AMP_INDEX], [2, B], label)
+        net.node_layers[label] = -1
+        NW.save_tensor_data(net, label, data)
+        net.edges[index].dst = label
+
+
+def run_uneven(args):
+    """Batched uneven workload: ``--circuits`` seeded random grid circuits
+    (qubits uniform in 12..30, grid factorised from the count, depth uniform
+    in 8..24), 64 random-bitstring amplitudes each.  Per circuit the cheaper
+    of two strategies by a roofline estimate: the state vector (single-qubit
+    gates fused into two-qubit gates, gate-by-gate order, the 64 amplitudes
+    gathered) or the qubit-sweep tensor-network order with the 64 output
+    bitstrings as one batch index.  Every plan is compiled, captured as a CUDA
+    graph and launched from it; a step contracts all circuits.  The first
+    ``--check`` circuits are also run in complex128 for the error."""
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    from pqgb300 import circuits as CI
+    from pqgb300 import planning as PL
+
+    prec_name = args.precision if args.precision != "auto" else "ozaki"
+    prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
+    rng = np.random.default_rng(2026)
+    specs = [(int(rng.integers(12, 31)), int(rng.integers(8, 25))) for _ in range(args.circuits)]
+    t0 = time.perf_counter()
+    plans = []
+    for i, (n, d) in enumerate(specs):
+        r, c = CI.grid_shape(n)
+        gates = pq.random_grid_gates(r, c, d, seed=10_000 + i)
+        fused = CI.fuse_single_qubit_gates(gates)
+        bits = pq.random_bitstrings(n, 64, seed=20_000 + i)
+        t_sv = (2.0 ** n) * 16 * len(fused) / 6e12 + len(fused) * 4e-6
+        host = _HostStore()
+        hn = pq.build_network(n, gates, decompose=True, backend=host)
+        pq.add_input(hn, "0" * n)
+        batched_outputs(pq, hn, bits)
+        nodes, ranks, flat, dims, label_of = PL._leaf_arrays(hn, [AMP_INDEX])
+        sw, cm, mx = PL.sweep_steps(hn, nodes, [label_of[AMP_INDEX]], label_of, ranks, flat, dims)
+        t_sw = cm * 8 / 40e12 + len(sw) // 2 * 4e-6 if mx * 8 < 2 ** 34 else float("inf")
+        if t_sv <= t_sw:
+            plans.append(dict(kind="statevector", n=n, d=d, gates=fused, bits=bits, decompose=False, steps=None))
+        else:
+            plans.append(dict(kind="sweep", n=n, d=d, gates=gates, bits=bits, decompose=True, steps=sw))
+    t_plan = time.perf_counter() - t0
+
+    def networks(be, count=None):
+        # all circuits share one backend: node labels (the backend's tensor
+        # names) start at a distinct offset per circuit
+        from pqgb300 import network as NW
+
+        nets = []
+        for ci, p in enumerate(plans[:count]):
+            net = NW.TensorNetworkCircuit(p["n"], be)
+            net.counters["node"] = ci * 10_000_000
+            for U, qs in p["gates"]:
+                NW.add_gate(net, CI.operator_to_tensor(U), qs, decompose=p["decompose"])
+            pq.add_input(net, "0" * p["n"])
+            if p["kind"] == "sweep":
+                batched_outputs(pq, net, p["bits"])
+                nets.append((net, p["steps"], [AMP_INDEX]))
+            else:
+                nets.append((net, PL.statevector_steps(net), None))
+        return nets
+
+    def run_all(nets, count=None):
+        out = []
+        for (net, steps, oe), p in list(zip(nets, plans))[:count]:
+            plan = pq.NetworkPlan(net, steps=steps, out_edges=oe)
+            res = plan.capture()
+            if p["kind"] == "sweep":
+                a = np.asarray(net.backend.load_tensor_data(res)).reshape(-1)
+            else:
+                a = net.backend.gather(res, PL.bitstrings_to_index(p["bits"]))
+                net.backend.delete_tensor(res)
+            plan.close()
+            out.append(a)
+        return out
+
+    be = pq.GB300Backend(prec)
+    t1 = time.perf_counter()
+    nets = networks(be)
+    t_build = time.perf_counter() - t1
+    for _ in range(min(1, args.warmup)):
+        run_all(nets)
+    be.sync()
+    ts, amps = [], None
+    for _ in range(max(1, args.steps)):
+        t1 = time.perf_counter()
+        amps = run_all(nets)
+        be.sync()
+        ts.append(time.perf_counter() - t1)
+    be.close()
+    # complex128 on the first circuits, same strategies
+    k = min(args.check, len(plans))
+    be64 = pq.GB300Backend(pq.PREC_C128)
+    ref = run_all(networks(be64, k), k) if k else []
+    be64.close()
+    errs = [float(np.max(np.abs(a - b)) / np.sqrt(np.mean(np.abs(b) ** 2))) for a, b in zip(amps[:k], ref)]
+    secs = sum(ts) / len(ts)
+    kinds = [p["kind"] for p in plans]
+    line = {"workload": f"uneven{args.circuits}_random_grid_circuits_64_amplitudes", "precision": prec_name,
+            "metric": "amplitudes/s (all circuits, 64 amplitudes each, compile + graph capture + run + read)",
+            "value": 64 * len(plans) / secs, "unit": "amplitudes/s", "higher_is_better": True,
+            "seconds_per_step": secs, "steps": len(ts), "circuits": len(plans),
+            "qubits_range": [min(p["n"] for p in plans), max(p["n"] for p in plans)],
+            "depth_range": [min(p["d"] for p in plans), max(p["d"] for p in plans)],
+            "strategies": {"statevector": kinds.count("statevector"), "sweep_batched": kinds.count("sweep")},
+            "host_planning_s": t_plan, "network_upload_s": t_build,
+            "checked_circuits": k, "max_err_over_rms_amplitude_vs_c128": max(errs) if errs else None,
+            "grouping": "one captured graph per circuit, launched in sequence (no cross-circuit kernel batching)",
+            "data": "synthetic (seeded random circuits)"}
+    print(json.dumps(line))
+    return 0
 
 
 def run_learned(args, rows=7, cols=7, depth=14):

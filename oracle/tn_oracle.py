@@ -748,8 +748,10 @@ def statevector(n, gates, init=None):
 def execute_ssa_plan(leaves, leaf_labels, steps, out_labels=()):
     """Execute SSA pair steps over numpy leaves with integer labels (the CPU
     equivalent of a compiled plan).  A label is summed once no other live
-    tensor and no output carries it; the result's modes follow ``out_labels``.
-    Each pair is one ``tensordot`` (BLAS zgemm), like TensorOperations->BLAS."""
+    tensor and no output carries it (so a label shared by more than two
+    tensors is a batch mode until its last use); the result's modes follow
+    ``out_labels``.  Each pair is one ``tensordot`` (BLAS zgemm), like
+    TensorOperations->BLAS, or one ``einsum`` when it keeps a shared label."""
     vals = [np.asarray(x) for x in leaves]
     labs = [list(l) for l in leaf_labels]
     cnt: dict[int, int] = {}
@@ -767,9 +769,18 @@ def execute_ssa_plan(leaves, leaf_labels, steps, out_labels=()):
             cnt[x] -= 1
         common = [x for x in la if x in lb]
         if any(cnt[x] > 0 for x in common):
-            raise ValueError("hyper-indices are not supported by the CPU plan executor")
-        C = np.tensordot(vals[a], vals[b], axes=([la.index(x) for x in common], [lb.index(x) for x in common]))
-        lc = [x for x in la if x not in common] + [x for x in lb if x not in common]
+            # a hyper index (carried by a third live tensor or the output) stays
+            # as a batch mode of this pair: one einsum with per-pair letters
+            keep = [x for x in dict.fromkeys(la + lb) if cnt[x] > 0]
+            letter = {x: chr(ord("a") + k) if k < 26 else chr(ord("A") + k - 26)
+                      for k, x in enumerate(dict.fromkeys(la + lb))}
+            spec = "".join(letter[x] for x in la) + "," + "".join(letter[x] for x in lb) + "->" + \
+                "".join(letter[x] for x in keep)
+            C = np.einsum(spec, vals[a], vals[b])
+            lc = keep
+        else:
+            C = np.tensordot(vals[a], vals[b], axes=([la.index(x) for x in common], [lb.index(x) for x in common]))
+            lc = [x for x in la if x not in common] + [x for x in lb if x not in common]
         for x in lc:
             cnt[x] += 1
         vals.append(C)

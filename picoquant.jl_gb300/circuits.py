@@ -88,6 +88,35 @@ def random_grid_gates(rows, cols, depth, seed):
     return g
 
 
+def fuse_single_qubit_gates(gates):
+    """The same circuit with every run of single-qubit gates folded into the
+    next two-qubit gate on that qubit (operator convention of
+    ``operator_to_tensor``: the first listed qubit is the low bit, so
+    U_a (x) U_b is kron(U_b, U_a)); single-qubit gates with no later two-qubit
+    gate are emitted at the end.  Exact; a state-vector order then sweeps the
+    state once per remaining gate."""
+    pending: dict[int, np.ndarray] = {}
+    out = []
+    for U, qs in gates:
+        U = np.asarray(U, dtype=np.complex128)
+        if len(qs) == 1:
+            q = qs[0]
+            pending[q] = U @ pending[q] if q in pending else U
+        elif len(qs) == 2:
+            a, b = qs
+            pa = pending.pop(a, np.eye(2, dtype=np.complex128))
+            pb = pending.pop(b, np.eye(2, dtype=np.complex128))
+            out.append((U @ np.kron(pb, pa), [a, b]))
+        else:
+            for q in qs:
+                if q in pending:
+                    out.append((pending.pop(q), [q]))
+            out.append((U, list(qs)))
+    for q in sorted(pending):
+        out.append((pending[q], [q]))
+    return out
+
+
 def grid_shape(n_qubits):
     """Most square rows x cols factorisation of a qubit count (rows <= cols)."""
     best = (1, n_qubits)

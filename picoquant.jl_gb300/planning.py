@@ -478,6 +478,37 @@ def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("swee
     return min(found, key=lambda t: (t[1], t[2]))
 
 
+def statevector_steps(network, leaves=None):
+    """SSA steps of a gate-by-gate state-vector order: the input vectors
+    folded into the state, then every gate node applied to the state in
+    creation (circuit) order, then the output vectors if any.  Unlike the
+    reference's layer order it never contracts a layer's gates together
+    first, so no intermediate exceeds the state's size."""
+    leaves = leaves if leaves is not None else list(network.nodes.keys())
+    pos = {lab: i for i, lab in enumerate(leaves)}
+    inputs = [pos[network.edges[e].src] for e in network.input_qubits]
+    steps = []
+    wf = inputs[0]
+    nxt = len(leaves)
+    for w in inputs[1:]:
+        steps += [wf, w]
+        wf = nxt
+        nxt += 1
+    in_set = set(inputs)
+    outs = [i for i, lab in enumerate(leaves) if network.node_layers.get(lab) == -1]
+    for i, lab in enumerate(leaves):
+        if i in in_set or i in outs:
+            continue
+        steps += [wf, i]
+        wf = nxt
+        nxt += 1
+    for o in outs:
+        steps += [wf, o]
+        wf = nxt
+        nxt += 1
+    return steps
+
+
 def wavefunction_steps(network, leaves=None):
     """SSA steps of the reference's default full-wavefunction order
     (src/layer2.jl:132-173): inputs folded left to right, then per layer the

@@ -157,3 +157,45 @@ def test_wavefunction_steps_match_reference_order(pq, O, host_backend):
     pq.contract_network(net, pq.steps_to_pairs(net, steps))
     out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
     assert np.max(np.abs(out - O.statevector(6, gates))) < 1e-13
+
+
+def test_fused_gates_statevector_order(pq, O, host_backend):
+    """Single-qubit gates folded into two-qubit gates, applied gate by gate
+    to the state: the state vector of the original circuit."""
+    from pqgb300 import circuits as CI
+
+    gates = pq.random_grid_gates(2, 3, 5, seed=4)
+    fused = CI.fuse_single_qubit_gates(gates)
+    assert len(fused) < len(gates) // 2
+    net = pq.build_network(6, fused, backend=host_backend)
+    pq.add_input(net, "0" * 6)
+    steps = pq.planning.statevector_steps(net)
+    _ssa_valid(steps, len(net.nodes))
+    pq.contract_network(net, pq.steps_to_pairs(net, steps))
+    out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
+    assert np.max(np.abs(out - O.statevector(6, gates))) < 1e-13
+
+
+def test_batched_output_amplitudes(pq, O, host_backend):
+    """Output tensors sharing one bitstring-batch index: one contraction of
+    the sweep order gives the amplitudes of all bitstrings."""
+    import bench
+
+    gates = pq.random_grid_gates(2, 3, 4, seed=6)
+    bits = pq.random_bitstrings(6, 5, seed=7)
+    net = pq.build_network(6, gates, backend=host_backend, decompose=True)
+    pq.add_input(net, "0" * 6)
+    bench.batched_outputs(pq, net, bits)
+    nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [bench.AMP_INDEX])
+    out = [label_of[bench.AMP_INDEX]]
+    steps, cm, mx = pq.planning.sweep_steps(net, nodes, out, label_of, ranks, flat, dims)
+    _ssa_valid(steps, len(nodes))
+    leaves = [host_backend.tensors[net.nodes[nl].data_label] for nl in nodes]
+    labs, pos = [], 0
+    for r in ranks:
+        labs.append(flat[pos:pos + r])
+        pos += r
+    amps = O.execute_ssa_plan(leaves, labs, steps, out)
+    sv = O.statevector(6, gates)
+    ref = np.array([sv[O.amplitude_index(b)] for b in bits])
+    assert np.max(np.abs(np.asarray(amps).reshape(-1) - ref)) < 1e-13
