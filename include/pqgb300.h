@@ -247,6 +247,18 @@ int pq_plan_greedy(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_
                    int n_labels, const int64_t* label_dims, int n_out, const int32_t* out_labels,
                    double alpha, double tau, int n_trials, uint64_t seed,
                    int32_t* steps, double* cmacs, int64_t* max_elems);
+/* `n_draws` independent planner draws (the candidates a learned cost model
+ * ranks): draw d samples with its own generator seeded by seed + d, draw 0
+ * with tau = 0 (plain greedy), the others with `tau`; they run on
+ * `n_threads` host threads (0: all hardware threads) and the results do not
+ * depend on the thread count.  Draw d's 2*(n_leaves-1) SSA operands go to
+ * steps[d*2*(n_leaves-1) ...], its cost to cmacs[d], its largest
+ * intermediate to max_elems[d].  Same planner as pq_plan_greedy
+ * (src/layer2/bgreedy_contraction.jl:17-66). */
+int pq_plan_greedy_many(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels,
+                        int n_labels, const int64_t* label_dims, int n_out, const int32_t* out_labels,
+                        double alpha, double tau, int n_draws, uint64_t seed, int n_threads,
+                        int32_t* steps, double* cmacs, int64_t* max_elems);
 /* Choose labels to slice: repeatedly fix the label that most reduces the
  * largest intermediate (ties: least flop increase) until the largest
  * intermediate is <= 2^log2_target elements or `max_sliced` labels are

@@ -19,7 +19,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib as L
-from .planning import (NetworkPlan, _leaf_arrays, greedy_steps, open_output_edges, plan_cost, sweep_steps,
+from .planning import (NetworkPlan, _leaf_arrays, greedy_draws, open_output_edges, plan_cost, sweep_steps,
                        wavefunction_steps)
 
 N_FEATURES = 5
@@ -245,21 +245,21 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
         out_edges = open_output_edges(network)
     nodes, ranks, flat, dims, label_of = _leaf_arrays(network, out_edges)
     outl = [label_of[e] for e in out_edges]
-    cands = []
+    out = []
+    # the sweep and native greedy planners return their own cost and largest
+    # intermediate (the same label rule as plan_cost)
     for i, (s, c, m) in enumerate(sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, all_orders=True)):
-        cands.append((f"sweep{i}", s))
+        out.append({"name": f"sweep{i}", "steps": s, "cmacs": c, "max_elems": m})
     if not out_edges or all(network.edges[e].src is not None for e in network.input_qubits):
         try:
-            cands.append(("wavefunction", wavefunction_steps(network, nodes)))
+            s = wavefunction_steps(network, nodes)
+            cost, mx = plan_cost(ranks, flat, dims, s, outl)
+            out.append({"name": "wavefunction", "steps": s, "cmacs": cost, "max_elems": mx})
         except KeyError:
             pass
-    for i in range(n_random):
-        s, _, _ = greedy_steps(ranks, flat, dims, outl, 1.0, 0.0 if i == 0 else 1.0, 1, seed + i)
-        cands.append((f"greedy{i}", s))
-    out = []
-    for name, s in cands:
-        cost, mx = plan_cost(ranks, flat, dims, s, outl)
-        out.append({"name": name, "steps": s, "cmacs": cost, "max_elems": mx})
+    if n_random > 0:
+        for i, (s, c, m) in enumerate(greedy_draws(ranks, flat, dims, outl, n_random, 1.0, 1.0, seed)):
+            out.append({"name": f"greedy{i}", "steps": s, "cmacs": c, "max_elems": m})
     return out, out_edges
 
 

@@ -17,6 +17,7 @@
 #include <map>
 #include <random>
 #include <set>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -62,8 +63,12 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
   }
   for (int x : out_labels) cnt[x]++;
   Trial t;
-  // candidate scores, keyed by (a, b) with a < b
-  std::map<std::pair<int, int>, double> cand;
+  // candidate pairs (a < b) that share a label, with their energies, and the
+  // same pairs ordered by energy: the minimum and the pairs near it (the
+  // only ones with a weight that matters) are read from the front
+  using Key = std::pair<int, int>;
+  std::map<Key, double> cand;
+  std::set<std::pair<double, Key>> order;
   auto result_labels = [&](int a, int b, std::vector<int>& r, double& l2c, double& l2all) {
     r.clear();
     l2all = 0;
@@ -86,43 +91,60 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
     result_labels(a, b, tmp, l2c, l2all);
     return std::exp2(l2c) - alpha * (std::exp2(l2[a]) + std::exp2(l2[b]));
   };
-  auto add_pairs_of = [&](int v) {
-    std::set<int> nb;
+  auto set_score = [&](int u, int v) {
+    const Key k(std::min(u, v), std::max(u, v));
+    auto it = cand.find(k);
+    if (it != cand.end()) order.erase({it->second, k});
+    const double e = score(k.first, k.second);
+    cand[k] = e;
+    order.insert({e, k});
+  };
+  auto erase_key = [&](int u, int v) {
+    const Key k(std::min(u, v), std::max(u, v));
+    auto it = cand.find(k);
+    if (it == cand.end()) return;
+    order.erase({it->second, k});
+    cand.erase(it);
+  };
+  // live values sharing a label with v
+  auto partners = [&](int v, std::vector<int>& nb) {
+    nb.clear();
     for (int x : lab[v])
       for (int u : holders[x])
-        if (u != v && live[u]) nb.insert(u);
-    for (int u : nb) {
-      auto key = std::make_pair(std::min(u, v), std::max(u, v));
-      cand[key] = score(key.first, key.second);
-    }
+        if (u != v && live[u]) nb.push_back(u);
+    std::sort(nb.begin(), nb.end());
+    nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
   };
-  for (int i = 0; i < nl; ++i) add_pairs_of(i);
+  std::vector<int> nb, nb2;
+  for (int i = 0; i < nl; ++i) {
+    partners(i, nb);
+    for (int u : nb)
+      if (u > i) set_score(i, u);
+  }
   int next = nl;
   int nlive = nl;
   std::uniform_real_distribution<double> U(0.0, 1.0);
-  std::vector<std::pair<int, int>> keys;
+  std::vector<Key> keys;
   std::vector<double> w;
   while (nlive > 1) {
     int a = -1, b = -1;
-    if (!cand.empty()) {
-      double emin = INFINITY;
-      for (auto& kv : cand) emin = std::min(emin, kv.second);
+    if (!order.empty()) {
+      const double emin = order.begin()->first;
+      keys.clear();
       if (tau <= 0) {
         // deterministic greedy with random tie-break
-        keys.clear();
-        for (auto& kv : cand)
-          if (kv.second <= emin) keys.push_back(kv.first);
+        for (auto it = order.begin(); it != order.end() && it->first <= emin; ++it) keys.push_back(it->second);
         auto k = keys[std::uniform_int_distribution<size_t>(0, keys.size() - 1)(rng)];
         a = k.first;
         b = k.second;
       } else {
+        // weights exp(-(e - emin) / T); pairs beyond 50 T weigh < e^-50
         const double T = tau * std::max(1.0, std::fabs(emin));
-        keys.clear();
         w.clear();
         double tot = 0;
-        for (auto& kv : cand) {
-          double x = std::exp(-(kv.second - emin) / T);
-          keys.push_back(kv.first);
+        for (auto it = order.begin(); it != order.end() && it->first - emin <= 50.0 * T; ++it) {
+          const double x = std::exp(-(it->first - emin) / T);
+          keys.push_back(it->second);
           w.push_back(x);
           tot += x;
         }
@@ -157,16 +179,14 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
     t.max_l2 = std::max(t.max_l2, l2c);
     t.steps.push_back(a);
     t.steps.push_back(b);
-    // retire a, b
+    // retire a, b and every candidate pair that holds one of them
+    partners(a, nb);
+    for (int u : nb) erase_key(a, u);
+    partners(b, nb);
+    for (int u : nb) erase_key(b, u);
     live[a] = live[b] = 0;
     for (int x : lab[a]) cnt[x]--;
     for (int x : lab[b]) cnt[x]--;
-    for (auto it = cand.begin(); it != cand.end();) {
-      if (it->first.first == a || it->first.second == a || it->first.first == b || it->first.second == b)
-        it = cand.erase(it);
-      else
-        ++it;
-    }
     int v = next++;
     lab[v] = r;
     l2[v] = l2c;
@@ -178,16 +198,15 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
       h.push_back(v);
     }
     nlive--;
-    // scores of pairs sharing a label whose count changed are stale; refresh
-    // every candidate touching a neighbour of v, then add v's pairs
-    std::set<int> touched;
-    for (int x : r)
-      for (int u : holders[x])
-        if (u != v && live[u]) touched.insert(u);
-    for (auto& kv : cand)
-      if (touched.count(kv.first.first) || touched.count(kv.first.second))
-        kv.second = score(kv.first.first, kv.first.second);
-    add_pairs_of(v);
+    // the counts of v's labels changed: every pair of a live value holding
+    // one of them is rescored, then v's own pairs are added
+    partners(v, nb);
+    for (int u : nb) {
+      partners(u, nb2);
+      for (int x : nb2)
+        if (x != v) set_score(u, x);
+    }
+    for (int u : nb) set_score(v, u);
   }
   return t;
 }
@@ -231,6 +250,56 @@ int pq_plan_greedy(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_
   if (n_leaves > 1) std::memcpy(steps, best.steps.data(), best.steps.size() * sizeof(int32_t));
   if (cmacs) *cmacs = n_leaves > 1 ? best.cmacs : 0.0;
   if (max_elems) *max_elems = (int64_t)std::llround(std::exp2(best.max_l2));
+  return PQ_OK;
+}
+
+int pq_plan_greedy_many(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                        const int64_t* label_dims, int n_out, const int32_t* out_labels, double alpha, double tau,
+                        int n_draws, uint64_t seed, int n_threads, int32_t* steps, double* cmacs,
+                        int64_t* max_elems) {
+  if (n_leaves < 1 || !leaf_ranks || (n_labels && !label_dims) || (n_out && !out_labels) || n_draws < 1 ||
+      (n_leaves > 1 && !steps) || !cmacs || !max_elems)
+    return PQ_ERR_INVALID;
+  std::vector<double> l2dim(n_labels);
+  for (int i = 0; i < n_labels; ++i) {
+    if (label_dims[i] < 1) return PQ_ERR_INVALID;
+    l2dim[i] = std::log2((double)label_dims[i]);
+  }
+  std::vector<std::vector<int>> leaves(n_leaves);
+  int pos = 0;
+  for (int i = 0; i < n_leaves; ++i) {
+    if (leaf_ranks[i] < 0) return PQ_ERR_INVALID;
+    for (int j = 0; j < leaf_ranks[i]; ++j) {
+      int x = leaf_labels[pos++];
+      if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+      leaves[i].push_back(x);
+    }
+  }
+  std::vector<int> outl(out_labels, out_labels + n_out);
+  for (int x : outl)
+    if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+  const size_t per = n_leaves > 1 ? (size_t)(2 * (n_leaves - 1)) : 0;
+  // draw d: its own generator seeded with seed + d, so results do not depend
+  // on the thread count; draw 0 is the plain greedy order (tau = 0)
+  auto run = [&](int d) {
+    std::mt19937_64 rng(seed + (uint64_t)d);
+    Trial tr = greedy_once(n_leaves, leaves, l2dim, outl, alpha, d == 0 ? 0.0 : tau, rng);
+    if (per) std::memcpy(steps + per * (size_t)d, tr.steps.data(), per * sizeof(int32_t));
+    cmacs[d] = per ? tr.cmacs : 0.0;
+    max_elems[d] = (int64_t)std::llround(std::exp2(tr.max_l2));
+  };
+  int nt = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min(nt, n_draws);
+  if (nt <= 1) {
+    for (int d = 0; d < n_draws; ++d) run(d);
+    return PQ_OK;
+  }
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      for (int d = t; d < n_draws; d += nt) run(d);
+    });
+  for (auto& th : pool) th.join();
   return PQ_OK;
 }
 

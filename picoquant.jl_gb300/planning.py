@@ -66,6 +66,25 @@ def greedy_steps(ranks, flat, dims, out_labels, alpha=1.0, tau=1.0, trials=10, s
     return [int(x) for x in steps[: 2 * (n - 1)]], cm.value, mx.value
 
 
+def greedy_draws(ranks, flat, dims, out_labels, n_draws, alpha=1.0, tau=1.0, seed=0, threads=0):
+    """``n_draws`` independent native planner draws (draw 0 plain greedy, the
+    others Boltzmann-sampled with ``tau``), run on host threads; returns a
+    list of (steps, cmacs, max_elems)."""
+    lib = L.lib()
+    n = len(ranks)
+    per = max(0, 2 * (n - 1))
+    steps = (C.c_int32 * max(1, per * n_draws))()
+    cm = (C.c_double * n_draws)()
+    mx = (C.c_int64 * n_draws)()
+    rc = lib.pq_plan_greedy_many(n, L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
+                                 L.arr(C.c_int64, dims), len(out_labels), L.arr(C.c_int32, out_labels),
+                                 float(alpha), float(tau), int(n_draws), int(seed) & ((1 << 64) - 1), int(threads),
+                                 steps, cm, mx)
+    L.check(rc, None, "pq_plan_greedy_many")
+    flat_steps = [int(x) for x in steps[: per * n_draws]]
+    return [(flat_steps[d * per:(d + 1) * per], cm[d], mx[d]) for d in range(n_draws)]
+
+
 def steps_to_pairs(network, steps, leaves=None):
     """SSA steps -> pair plan of node labels as contract_pair! will name them
     (results are node_<counter+1>, node_<counter+2>, ...)."""

@@ -199,3 +199,24 @@ def test_batched_output_amplitudes(pq, O, host_backend):
     sv = O.statevector(6, gates)
     ref = np.array([sv[O.amplitude_index(b)] for b in bits])
     assert np.max(np.abs(np.asarray(amps).reshape(-1) - ref)) < 1e-13
+
+
+def test_greedy_draws_parallel_deterministic(pq, host_backend):
+    """Parallel planner draws: valid SSA plans whose costs match the host
+    cost function; draw 0 is the plain greedy order; results do not depend
+    on the thread count; the Boltzmann draws vary."""
+    gates = pq.random_grid_gates(3, 3, 6, seed=3)
+    net = pq.build_network(9, gates, backend=host_backend, decompose=True)
+    pq.add_input(net, "0" * 9)
+    pq.add_output(net, "010011010")
+    nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
+    d1 = pq.planning.greedy_draws(ranks, flat, dims, [], 12, seed=5, threads=1)
+    d4 = pq.planning.greedy_draws(ranks, flat, dims, [], 12, seed=5, threads=4)
+    assert [x[0] for x in d1] == [x[0] for x in d4]
+    for s, cm, mx in d1:
+        _ssa_valid(s, len(ranks))
+        c2, m2 = pq.planning.plan_cost(ranks, flat, dims, s, [])
+        assert abs(cm - c2) <= 1e-9 * c2 and m2 == mx
+    s0, _, _ = pq.greedy_steps(ranks, flat, dims, [], 1.0, 1.0, 1, 5)
+    assert d1[0][0] == s0
+    assert len({tuple(x[0]) for x in d1}) > 1
