@@ -315,6 +315,19 @@ class NetworkPlan:
         return [inv[out[i]] for i in range(n.value)]
 
 
+def slice_range(total, rank, world):
+    """Contiguous, balanced share [begin, end) of ``total`` slices for rank
+    ``rank`` of ``world`` (the multi-GPU split of a sliced contraction: each
+    rank runs ``NetworkPlan.run_sliced(..., begin, end)`` and one reduction
+    of the partial sums finishes the amplitude, as the reference's
+    examples/dist_slicing_example.jl:30 reduces partition results)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must be in [0, world)")
+    base, extra = divmod(int(total), int(world))
+    begin = rank * base + min(rank, extra)
+    return begin, begin + base + (1 if rank < extra else 0)
+
+
 def bitstrings_to_index(bitstrings):
     """Column-major linear index of each bitstring (character i -> bit i)."""
     out = np.empty(len(bitstrings), dtype=np.int64)
