@@ -715,8 +715,7 @@ def run_gb300(args, world, rank):
         h2d = sum(a.nbytes for _, a in host)
 
         def e2e_step():
-            for lab, a in host:
-                be.save_tensor_data(lab, a)
+            be.save_tensors(host)  # every leaf, one staging copy + one device scatter
             return plan.run_sliced(sliced, batch=args.batch)
 
         e2e_step()

@@ -110,6 +110,17 @@ int pq_ctx_stream(pq_ctx* ctx, void** stream);
  * storage type on upload.  Replaces an existing tensor with the same id. */
 int pq_save_tensor_data(pq_ctx* ctx, int64_t id, int rank, const int64_t* dims,
                         const void* data, int dtype);
+/* Upload n tensors in one batch (no reference counterpart: an extension
+ * for hosts that re-upload many small tensors per contraction, e.g. every
+ * gate of a circuit).  Same semantics per tensor as pq_save_tensor_data
+ * (ids[i], ranks[i] extents taken in order from dims_flat, column-major host
+ * data[i] of type dtypes[i], stored in the context's storage type); all data
+ * go through one pinned staging buffer, one host-to-device copy and one
+ * device scatter, and a tensor replaced by one of the same extents keeps its
+ * device storage.  The host arrays may be reused as soon as the call
+ * returns. */
+int pq_save_tensors(pq_ctx* ctx, int n, const int64_t* ids, const int32_t* ranks, const int64_t* dims_flat,
+                    const void* const* data, const int32_t* dtypes);
 /* src/backends/interactive.jl:44-49 `load_tensor_data`.  Copies the tensor to
  * host memory as `dtype` (dst must hold `n_elems` elements, n_elems >= size).
  * Returns PQ_ERR_NOT_FOUND when the id is absent (the reference returns

@@ -68,6 +68,7 @@ SIGNATURES = [
     ("pq_ctx_set_small_elems", C.c_int, [vp, C.c_int64]),
     ("pq_ctx_stream", C.c_int, [vp, C.POINTER(vp)]),
     ("pq_save_tensor_data", C.c_int, [vp, C.c_int64, C.c_int, i64p, vp, C.c_int]),
+    ("pq_save_tensors", C.c_int, [vp, C.c_int, i64p, i32p, i64p, C.POINTER(C.c_void_p), i32p]),
     ("pq_load_tensor_data", C.c_int, [vp, C.c_int64, vp, C.c_int64, C.c_int]),
     ("pq_tensor_shape", C.c_int, [vp, C.c_int64, C.POINTER(C.c_int), i64p]),
     ("pq_has_tensor", C.c_int, [vp, C.c_int64]),

@@ -138,6 +138,31 @@ class GB300Backend:
                                           a.ctypes.data_as(C.c_void_p), dt)
         self._check(rc, f"save_tensor_data({label})")
 
+    def save_tensors(self, items):
+        """Upload several (label, array) pairs in one batch (``pq_save_tensors``:
+        one staging copy and one device scatter instead of one copy each)."""
+        items = list(items)
+        if not items:
+            return
+        arrs, ids, ranks, dims, dts = [], [], [], [], []
+        for label, data in items:
+            a = np.asarray(data)
+            shape = a.shape
+            if a.dtype == np.complex64:
+                a = np.asfortranarray(a)
+                dts.append(L.PQ_C64)
+            else:
+                a = np.asfortranarray(a, dtype=np.complex128)
+                dts.append(L.PQ_C128)
+            arrs.append(a)
+            ids.append(self.id_of(label))
+            ranks.append(len(shape))
+            dims.extend(shape)
+        ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        rc = self.lib.pq_save_tensors(self.ctx, len(arrs), L.arr(C.c_int64, ids), L.arr(C.c_int32, ranks),
+                                      L.arr(C.c_int64, dims or [0]), ptrs, L.arr(C.c_int32, dts))
+        self._check(rc, "save_tensors")
+
     def has_tensor(self, label) -> bool:
         key = str(label)
         return key in self._ids and bool(self.lib.pq_has_tensor(self.ctx, self._ids[key]))

@@ -160,7 +160,10 @@ int pq_ctx_destroy(pq_ctx* c) {
   cudaSetDevice(ctx->device);
   for (auto& kv : ctx->tensors) free_tensor(ctx, kv.second);
   ctx->tensors.clear();
+  if (ctx->d_stage) dev_free(ctx, ctx->d_stage, ctx->d_stage_cap);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->stage_done) cudaEventDestroy(ctx->stage_done);
   cudaFree(ctx->d_status);
   cudaMemPoolDestroy(ctx->pool);
   cudaStreamDestroy(ctx->stream);
@@ -233,6 +236,95 @@ int pq_save_tensor_data(pq_ctx* c, int64_t id, int rank, const int64_t* dims, co
     return cuda_fail(ctx, e, "save_tensor_data upload");
   }
   put_entry(ctx, id, std::move(t));
+  return PQ_OK;
+}
+
+int pq_save_tensors(pq_ctx* c, int n, const int64_t* ids, const int32_t* ranks, const int64_t* dims_flat,
+                    const void* const* data, const int32_t* dtypes) {
+  CTX_OR_FAIL(c);
+  if (n < 0 || (n > 0 && (!ids || !ranks || !data || !dtypes)))
+    return fail(ctx, PQ_ERR_INVALID, "save_tensors: bad arguments");
+  if (n == 0) return PQ_OK;
+  // validate and lay out: data in the storage type, each at a 16-byte offset,
+  // then the copy table
+  std::vector<std::vector<int64_t>> dims(n);
+  std::vector<int> sdt(n);
+  std::vector<size_t> off(n), bytes(n);
+  size_t pos = 0, dpos = 0;
+  for (int i = 0; i < n; ++i) {
+    if (ranks[i] < 0 || ranks[i] > PQ_MAX_RANK || !data[i] || (ranks[i] > 0 && !dims_flat))
+      return fail(ctx, PQ_ERR_INVALID, "save_tensors: bad rank/data of tensor " + std::to_string(i));
+    if (dtypes[i] != PQ_C64 && dtypes[i] != PQ_C128)
+      return fail(ctx, PQ_ERR_INVALID, "save_tensors: bad dtype of tensor " + std::to_string(i));
+    dims[i].assign(dims_flat + dpos, dims_flat + dpos + ranks[i]);
+    dpos += ranks[i];
+    for (auto x : dims[i])
+      if (x < 1) return fail(ctx, PQ_ERR_INVALID, "save_tensors: extents must be >= 1");
+    const int64_t size = prod(dims[i]);
+    sdt[i] = storage_dtype(ctx, size);
+    bytes[i] = (size_t)size * elem_bytes(sdt[i]);
+    off[i] = pos;
+    pos += (bytes[i] + 15) & ~(size_t)15;
+  }
+  {
+    std::vector<int64_t> sorted_ids(ids, ids + n);
+    std::sort(sorted_ids.begin(), sorted_ids.end());
+    if (std::adjacent_find(sorted_ids.begin(), sorted_ids.end()) != sorted_ids.end())
+      return fail(ctx, PQ_ERR_INVALID, "save_tensors: an id appears twice in one batch");
+  }
+  const size_t table_off = pos;
+  const size_t total = table_off + (size_t)n * sizeof(CopyJob);
+  cudaError_t e = cudaSuccess;
+  if (ctx->stage_done) {
+    e = cudaEventSynchronize(ctx->stage_done);  // the previous batch has left the host buffer
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "save_tensors wait");
+  } else if ((e = cudaEventCreateWithFlags(&ctx->stage_done, cudaEventDisableTiming)) != cudaSuccess) {
+    return cuda_fail(ctx, e, "save_tensors event");
+  }
+  if (total > ctx->h_stage_cap) {
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_cap = 0;
+    const size_t cap = total + total / 2;
+    if ((e = cudaHostAlloc(&ctx->h_stage, cap, cudaHostAllocDefault)) != cudaSuccess)
+      return cuda_fail(ctx, e, "save_tensors pinned staging");
+    ctx->h_stage_cap = cap;
+  }
+  if (total > ctx->d_stage_cap) {
+    if (ctx->d_stage) dev_free(ctx, ctx->d_stage, ctx->d_stage_cap);
+    ctx->d_stage = nullptr;
+    ctx->d_stage_cap = 0;
+    const size_t cap = total + total / 2;
+    int st = dev_alloc(ctx, cap, &ctx->d_stage);
+    if (st) return st;
+    ctx->d_stage_cap = cap;
+  }
+  unsigned char* h = (unsigned char*)ctx->h_stage;
+  CopyJob* jobs = (CopyJob*)(h + table_off);
+  for (int i = 0; i < n; ++i) {
+    const int64_t size = prod(dims[i]);
+    if (dtypes[i] == sdt[i])
+      std::memcpy(h + off[i], data[i], bytes[i]);
+    else
+      convert_host(data[i], dtypes[i], h + off[i], sdt[i], size);
+    // a tensor replaced by one of the same extents and type keeps its storage
+    auto it = ctx->tensors.find(ids[i]);
+    if (it != ctx->tensors.end() && it->second.dims == dims[i] && it->second.dtype == sdt[i] && it->second.ptr) {
+      jobs[i] = CopyJob{(int64_t)off[i], it->second.ptr, (int64_t)bytes[i]};
+      continue;
+    }
+    Tensor t;
+    int st = alloc_tensor(ctx, dims[i], sdt[i], t);
+    if (st) return st;
+    jobs[i] = CopyJob{(int64_t)off[i], t.ptr, (int64_t)bytes[i]};
+    put_entry(ctx, ids[i], std::move(t));
+  }
+  e = cudaMemcpyAsync(ctx->d_stage, h, total, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->stage_done, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_scatter(ctx->d_stage, (const CopyJob*)((unsigned char*)ctx->d_stage + table_off), n, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "save_tensors upload");
+  ctx->launches += 1;
   return PQ_OK;
 }
 

@@ -97,6 +97,14 @@ struct Ctx {
   int64_t mem_cap = 0;
   int64_t mem_in_use = 0;
   int64_t launches = 0;
+  // batched uploads (pq_save_tensors): pinned host and device staging,
+  // reused across calls; the host side is rewritten only after the event of
+  // the previous batch's copy has completed
+  void* h_stage = nullptr;
+  size_t h_stage_cap = 0;
+  void* d_stage = nullptr;
+  size_t d_stage_cap = 0;
+  cudaEvent_t stage_done = nullptr;
   // Mixed-precision contexts store tensors of at most this many elements as
   // complex128 (gates, per-qubit tensors: cheap, and their rounding would
   // dominate the error) and larger ones as complex64.
@@ -131,6 +139,14 @@ cudaError_t launch_permute(int tin, int tout, const void* in, int64_t base, void
                            const GenericDesc& d, cudaStream_t stream);
 cudaError_t launch_gather(int dt, const void* in, const int64_t* d_idx, int64_t n,
                           void* out, cudaStream_t stream);
+// One launch copying n byte ranges from a device staging buffer to their
+// destinations (src offsets 16-byte aligned).
+struct CopyJob {
+  int64_t src_off;
+  void* dst;
+  int64_t bytes;
+};
+cudaError_t launch_scatter(const void* src, const CopyJob* d_jobs, int n, cudaStream_t stream);
 // Batched leaf gather for slicing: out[x + xs*b] = in[x_off(x) + slice_off(s0+b)]
 // for b < nb, where x runs over `d` (csa = input strides of the kept modes)
 // and the slice offset is the mixed-radix digits of (s0+b) over the sliced

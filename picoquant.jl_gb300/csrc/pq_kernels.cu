@@ -215,6 +215,28 @@ cudaError_t launch_gather(int dt, const void* in, const int64_t* d_idx, int64_t 
   return cudaGetLastError();
 }
 
+// One block per job (grid-stride over jobs): 16-byte vector copies, an
+// 8-byte tail by thread 0.
+__global__ void __launch_bounds__(256) k_scatter(const unsigned char* __restrict__ src,
+                                                 const CopyJob* __restrict__ jobs, int n) {
+  for (int j = blockIdx.x; j < n; j += gridDim.x) {
+    const CopyJob cj = jobs[j];
+    const uint4* s = reinterpret_cast<const uint4*>(src + cj.src_off);
+    uint4* d = reinterpret_cast<uint4*>(cj.dst);
+    const int64_t n16 = cj.bytes / 16;
+    for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+    if (threadIdx.x == 0 && (cj.bytes & 15))
+      reinterpret_cast<uint2*>(cj.dst)[2 * n16] = reinterpret_cast<const uint2*>(src + cj.src_off)[2 * n16];
+  }
+}
+
+cudaError_t launch_scatter(const void* src, const CopyJob* d_jobs, int n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = n < 152 * 8 ? n : 152 * 8;
+  k_scatter<<<grid, 256, 0, stream>>>((const unsigned char*)src, d_jobs, n);
+  return cudaGetLastError();
+}
+
 struct SliceTab {
   int n;
   int64_t dim[kMaxModes];
