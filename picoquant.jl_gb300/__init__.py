@@ -18,7 +18,7 @@ from .contraction import (contract_network, contract_pair, create_ncon_indices, 
 from .network import (Edge, Node, TensorNetworkCircuit, add_gate, add_input, add_output, decompose_gate,
                       delete_tensor, edges, getedge, getnode, inedges, inneighbours, load_tensor_data, neighbours,
                       new_label, outedges, outneighbours, permute_tensor, reshape_tensor, save_output,
-                      save_tensor_data, view_tensor, virtualedges, virtualneighbours)
+                      save_tensor_data, view_tensor, virtualedges, virtualneighbours, network_from_dict, network_from_json, to_dict, to_json)
 from .planning import (NetworkPlan, bgreedy, bgreedy_contraction, bitstrings_to_index, greedy_steps,
                        open_output_edges, pairs_to_steps, steps_to_pairs, wavefunction_steps)
 

@@ -248,3 +248,79 @@ def outedges(network, node_label):
 
 def virtualedges(network, node_label):
     return [x for x in network.nodes[node_label].indices if network.edges[x].virtual]
+
+
+# ---- serialisation (src/layer3.jl:579-707) ----------------------------------
+# Same keys and value formats as the reference, so a network description moves
+# between the two implementations: edges {src, dst, virtual, qubit}; nodes
+# {indices, dims (as strings), data_label}; the tensor data stay in the backend.
+
+def edge_to_dict(edge: Edge) -> dict:
+    """src/layer3.jl:584-587."""
+    return {"src": edge.src, "dst": edge.dst, "virtual": edge.virtual, "qubit": edge.qubit}
+
+
+def edge_from_dict(d) -> Edge:
+    """src/layer3.jl:594-599."""
+    return Edge(d["src"], d["dst"], d["qubit"], d["virtual"])
+
+
+def node_to_dict(node: Node) -> dict:
+    """src/layer3.jl:606-611."""
+    return {"indices": [str(x) for x in node.indices], "dims": [str(int(x)) for x in node.dims],
+            "data_label": str(node.data_label)}
+
+
+def node_from_dict(d) -> Node:
+    """src/layer3.jl:618-623."""
+    return Node([str(x) for x in d["indices"]], [int(x) for x in d["dims"]], str(d["data_label"]))
+
+
+def to_dict(network: TensorNetworkCircuit) -> dict:
+    """src/layer3.jl:630-647 (key order kept)."""
+    return {
+        "number_qubits": network.number_qubits,
+        "edges": {str(k): edge_to_dict(v) for k, v in network.edges.items()},
+        "nodes": {str(k): node_to_dict(v) for k, v in network.nodes.items()},
+        "input_qubits": [str(x) for x in network.input_qubits],
+        "output_qubits": [str(x) for x in network.output_qubits],
+        "qubit_ordering": [int(x) for x in network.qubit_ordering],
+        "node_layers": {str(k): int(v) for k, v in network.node_layers.items()},
+    }
+
+
+def network_from_dict(d, backend=None) -> TensorNetworkCircuit:
+    """src/layer3.jl:654-681: the graph of ``d`` on ``backend`` (whose tensor
+    store must hold the nodes' data labels); the label counters continue
+    after the largest node and index numbers present."""
+    net = TensorNetworkCircuit(int(d["number_qubits"]), backend)
+    net.edges = {}
+    index = 0
+    for k, v in d["edges"].items():
+        index = max(index, int(k.split("_")[-1]))
+        net.edges[k] = edge_from_dict(v)
+    net.nodes = {}
+    node = 0
+    for k, v in d["nodes"].items():
+        node = max(node, int(k.split("_")[-1]))
+        net.nodes[k] = node_from_dict(v)
+    net.input_qubits = [str(x) for x in d["input_qubits"]]
+    net.output_qubits = [str(x) for x in d["output_qubits"]]
+    net.qubit_ordering = [int(x) for x in d["qubit_ordering"]]
+    net.node_layers = {str(k): int(v) for k, v in d["node_layers"].items()}
+    net.counters = {"index": index, "node": node, "layer": max([0, *net.node_layers.values()])}
+    return net
+
+
+def to_json(network: TensorNetworkCircuit, indent: int = 0) -> str:
+    """src/layer3.jl:688-695."""
+    import json
+
+    return json.dumps(to_dict(network), indent=indent if indent else None)
+
+
+def network_from_json(json_str: str, backend=None) -> TensorNetworkCircuit:
+    """src/layer3.jl:702-705."""
+    import json
+
+    return network_from_dict(json.loads(json_str), backend)

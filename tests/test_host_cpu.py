@@ -220,3 +220,27 @@ def test_greedy_draws_parallel_deterministic(pq, host_backend):
     s0, _, _ = pq.greedy_steps(ranks, flat, dims, [], 1.0, 1.0, 1, 5)
     assert d1[0][0] == s0
     assert len({tuple(x[0]) for x in d1}) > 1
+
+
+def test_network_json_round_trip(pq, O, host_backend):
+    """src/layer3.jl:579-707: to_json / network_from_json keep the graph (and
+    the reference's value formats); the round-tripped network contracts to
+    the same GHZ-3 amplitude (test/layer1_tests.jl:34-39)."""
+    import json
+
+    net = pq.build_network(3, pq.ghz_gates(3), backend=host_backend, decompose=True)
+    pq.add_input(net, "000")
+    pq.add_output(net, "000")
+    s = pq.to_json(net, 2)
+    d = json.loads(s)
+    assert list(d) == ["number_qubits", "edges", "nodes", "input_qubits", "output_qubits", "qubit_ordering",
+                       "node_layers"]
+    assert all(isinstance(x, str) for v in d["nodes"].values() for x in v["dims"])
+    net2 = pq.network_from_json(s, host_backend)
+    assert pq.to_dict(net2) == pq.to_dict(net)
+    assert net2.counters["node"] == max(int(k.split("_")[-1]) for k in net.nodes)
+    # a new node continues the numbering
+    assert pq.network.new_label(net2, "node") not in net.nodes
+    pq.contract_network(net2, pq.random_contraction_plan(net2, np.random.default_rng(0)))
+    amp = complex(np.asarray(pq.load_tensor_data(net2, "result")).reshape(-1)[0])
+    assert abs(amp - 1 / np.sqrt(2)) < 1e-12
