@@ -160,6 +160,28 @@ class OracleBackend:
     def view_tensor(self, view, node, bond_idx1, lo1, hi1):
         self.tensors[view] = tensor_view_array(self.tensors[node], bond_idx1, lo1, hi1)
 
+    def decompose_tensor(self, tensor, left_positions, right_positions, threshold=1e-13, max_rank=0,
+                         left_label=None, right_label=None):
+        """src/backends/interactive.jl:124-151 -> src/layer1.jl:146-184: SVD
+        across (left | right) positions (1-based); singular values kept while
+        s / ||s|| exceeds max(threshold, sqrt(eps)); returns the bond extent."""
+        t = self.tensors[tensor]
+        ld = [t.shape[x - 1] for x in left_positions]
+        rd = [t.shape[x - 1] for x in right_positions]
+        A = np.transpose(t, [x - 1 for x in list(left_positions) + list(right_positions)])
+        A = np.reshape(A, (int(np.prod(ld)), int(np.prod(rd))), order="F")
+        U, S, Vh = np.linalg.svd(A, full_matrices=False)
+        thr = max(threshold, float(np.sqrt(np.finfo(np.float64).eps)))
+        norm = float(np.sqrt(np.sum(S ** 2)))
+        chi = int(np.sum(S / norm > thr)) if norm > 0 else 0
+        if max_rank > 0:
+            chi = min(chi, max_rank)
+        sq = np.sqrt(S[:chi])
+        self.tensors[left_label] = np.reshape(U[:, :chi] * sq[None, :], tuple(ld) + (chi,), order="F")
+        self.tensors[right_label] = np.reshape(sq[:, None] * Vh[:chi, :], (chi,) + tuple(rd), order="F")
+        del self.tensors[tensor]
+        return chi
+
 
 # --------------------------------------------------------------------------
 # L3: tensor network circuit (src/layer3.jl)
