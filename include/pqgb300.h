@@ -230,7 +230,11 @@ int pq_plan_step_features(pq_plan* plan, double* feats);
  * output must be a scalar or small tensor; the running sum (n_out_elems
  * complex doubles, interleaved re/im, plus the same number of compensation
  * terms) lives on the device until `pq_sliced_result`.  Parts of the
- * contraction tree that touch no sliced leaf are computed once per call. */
+ * contraction tree that touch no sliced leaf are computed once per call.
+ * The run is recorded as a CUDA graph on the second consecutive call with the
+ * same leaf storage, sliced labels, range, batch and reset flag, and
+ * replayed from then on (new leaf data in the same storage, e.g. from
+ * pq_save_tensors, is read by the replay). */
 int pq_plan_run_sliced(pq_plan* plan, const int64_t* leaf_ids, int n_sliced,
                        const int32_t* sliced_labels, int64_t slice_begin, int64_t slice_end,
                        int batch, int reset_sum);

@@ -137,6 +137,40 @@ def test_sliced_single_amplitude(pq, O, prec, batch):
     be.close()
 
 
+def test_sliced_run_graph_replay(pq, O, prec):
+    """Repeated identical sliced runs: the second is captured as a CUDA graph
+    and later ones replay it; results stay the same, the launch count per
+    run stays the same, new leaf data in the same storage is picked up, and a
+    changed range runs directly again."""
+    r, c, d = 3, 4, 8
+    bits = "110100101101"
+    be = pq.GB300Backend(prec)
+    net, g = single_amp_net(pq, be, r, c, d, 7, bits)
+    steps, _, _, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    sliced = plan.choose_slices(max_sliced=4, log2_target=0)
+    amps, counts = [], []
+    for _ in range(4):
+        n0 = be.launch_count()
+        amps.append(plan.run_sliced(sliced, batch=4))
+        counts.append(be.launch_count() - n0)
+    assert len(set(counts)) == 1
+    assert max(abs(a - amps[0]) for a in amps) <= 1e-12 * abs(amps[0])
+    ref = O.statevector(r * c, g)[O.amplitude_index(bits)]
+    assert abs(amps[0] - ref) / 2.0 ** (-(r * c) / 2) < TOL[prec]
+    # scale one leaf in place (same extents: batched upload keeps its storage)
+    lab = net.nodes[plan.leaves[0]].data_label
+    data = be.load_tensor_data(lab)
+    be.save_tensors([(lab, 2 * data)])
+    assert abs(plan.run_sliced(sliced, batch=4) - 2 * amps[0]) <= 1e-9 * abs(amps[0])
+    # another range
+    total = 2 ** len(sliced)
+    part = plan.run_sliced(sliced, batch=4, begin=0, end=total // 2)
+    assert np.isfinite(part)
+    plan.close()
+    be.close()
+
+
 def test_config3_scaled_sliced(pq, O, prec):
     """Config 3 in miniature: 4x4 grid, depth 10, CZ split into bond-2
     virtual edges, 6 sliced bonds (64 identical-shape slices) summed in FP64."""
