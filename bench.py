@@ -315,8 +315,8 @@ def run_uneven(args):
 def run_learned(args, rows=7, cols=7, depth=14):
     """Learned plan selection for a 7x7 depth-14 random circuit (49 qubits),
     one amplitude: candidate orders (the qubit sweeps, the full-wavefunction
-    order and ``--candidates`` seeded random-greedy draws) ranked by the cost
-    model, the flop-count planner judging; slices chosen for the winner; the
+    order and ``--candidates`` seeded random-greedy draws) and, for each, its
+    slicing sets ranked by the cost model, the flop-count planner judging; the
     end-to-end time from the network to the amplitude (planning included) and
     the amplitudes of the learned and the flop-count plans and of the plain
     complex-FP64 path."""
@@ -352,10 +352,13 @@ def run_learned(args, rows=7, cols=7, depth=14):
     t0 = time.perf_counter()
     net = network(be)
     model = CM.CostModel.load(be)
-    chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=args.candidates)
+    # orders and slicing sets ranked together (unsliced, and the slice
+    # chooser at 2^target, 2^(target-2), 2^(target-4) elements)
+    chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=args.candidates,
+                                               slice_targets=(target, target - 2, target - 4), batch=1024)
     model.close()
     plan = pq.NetworkPlan(net, steps=chosen["steps"], out_edges=[])
-    sliced = plan.choose_slices(max_sliced=10, log2_target=target)
+    sliced = chosen.get("sliced", [])
     t_plan = time.perf_counter() - t0
     amp = amplitude(plan, sliced)
     t_e2e = time.perf_counter() - t0
@@ -398,7 +401,7 @@ def run_learned(args, rows=7, cols=7, depth=14):
             "flop_plan": {"name": best_flop["name"], "log2_cmacs": float(np.log2(best_flop["cmacs"])),
                           "seconds": t_flop},
             "candidates": len(cands), "candidates_within_flop_judge": len(ranked),
-            "model_ranking_top5": [(c["name"], c["pred_us"]) for c in ranked[:5]],
+            "model_ranking_top5": [(c["name"], c["pred_us"], len(c.get("sliced", []))) for c in ranked[:5]],
             "sliced_bonds": len(sliced), "slice_target_log2": target,
             "amplitude": [amp.real, amp.imag],
             "rel_diff_learned_vs_flop_plan": abs(amp - amp_f) / abs(amp_f),

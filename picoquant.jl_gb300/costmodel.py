@@ -263,19 +263,42 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
     return out, out_edges
 
 
-def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_factor=8.0, max_elems=2**30):
-    """Rank candidate plans by the model's predicted time.  The flop-count
-    planner judges: candidates more than ``flop_factor`` times the minimum
-    complex multiply-adds (or above ``max_elems``) are rejected, and the
-    flop-optimal plan is the fallback.  Returns (chosen, all candidates)."""
+def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_factor=8.0, max_elems=2**30,
+                 slice_targets=(), max_sliced=10, batch=1024):
+    """Rank candidate plans -- and, with ``slice_targets``, candidate slicing
+    sets of each (the slice chooser at each target, log2 elements, for plans
+    whose largest intermediate exceeds the largest target) -- by the model's
+    predicted time per amplitude.  The flop-count planner judges:
+    candidates more than ``flop_factor`` times the minimum complex
+    multiply-adds (or above ``max_elems`` without slicing) are rejected, and
+    the flop-optimal plan is the fallback.  Returns (chosen, flop-optimal
+    plan, all candidates); each candidate carries ``pred_us`` and, when
+    slicing sets were ranked, its best ``sliced`` edge list."""
     cands, out_edges = candidate_plans(network, out_edges, n_random, seed)
     best_flop = min(cands, key=lambda c: (c["cmacs"], c["max_elems"]))
     for c in cands:
-        if c["cmacs"] > flop_factor * best_flop["cmacs"] or c["max_elems"] > max_elems:
+        if c["cmacs"] > flop_factor * best_flop["cmacs"] or (c["max_elems"] > max_elems and not slice_targets):
             c["pred_us"] = float("inf")
             continue
         p = NetworkPlan(network, steps=c["steps"], out_edges=out_edges)
-        c["pred_us"] = float(model.predict_us(p.features()).sum())
+        if not slice_targets:
+            c["pred_us"] = float(model.predict_us(p.features()).sum())
+        else:
+            best = (float("inf"), None)
+            options = [[]] if c["max_elems"] <= max_elems else []
+            # slicing a plan whose intermediates already fit the largest
+            # target only adds work, so slicing sets are ranked when needed
+            if c["max_elems"] > 2.0 ** max(slice_targets):
+                for t in slice_targets:
+                    sl = p.choose_slices(max_sliced=max_sliced, log2_target=float(t))
+                    if sl not in options:
+                        options.append(sl)
+            for sl in options:
+                feats, reps = p.sliced_features(sl, batch)
+                t_us = float((model.predict_us(feats) * reps).sum())
+                if t_us < best[0]:
+                    best = (t_us, sl)
+            c["pred_us"], c["sliced"] = best
         p.close()
     chosen = min(cands, key=lambda c: c["pred_us"])
     if not np.isfinite(chosen["pred_us"]):

@@ -287,6 +287,52 @@ class NetworkPlan:
             out.append((sum(np.log2(self.dims[x]) for x in keep if x not in S), dep[-1]))
         return out
 
+    def sliced_features(self, sliced_edges, batch):
+        """Step features of the sliced execution (the cost model's inputs) and
+        how often each step runs per amplitude: the sliced labels are fixed,
+        steps that depend on a sliced leaf carry the batch of ``batch``
+        slices as an extra mode and run once per batch, the others once.
+        The unit-stride runs come from the unsliced plan."""
+        base = self.features()
+        S = {self.label_of[e] for e in sliced_edges}
+        total = 1
+        for x in S:
+            total *= self.dims[x]
+        nbatch = -(-total // batch) if S else 1
+        lb = float(np.log2(batch)) if S else 0.0
+        l2 = [float(np.log2(d)) for d in self.dims]
+        labs, dep, pos = [], [], 0
+        for r in self.ranks:
+            ll = self.flat[pos:pos + r]
+            pos += r
+            labs.append(ll)
+            dep.append(bool(set(ll) & S))
+        cnt: dict[int, int] = {}
+        for ll in labs:
+            for x in ll:
+                cnt[x] = cnt.get(x, 0) + 1
+        for x in self.out_labels:
+            cnt[x] = cnt.get(x, 0) + 1
+        feats = np.array(base, dtype=np.float64)
+        reps = np.ones(len(self.steps) // 2)
+        for i in range(len(self.steps) // 2):
+            a, b = self.steps[2 * i], self.steps[2 * i + 1]
+            for x in labs[a] + labs[b]:
+                cnt[x] -= 1
+            union = list(dict.fromkeys(labs[a] + labs[b]))
+            keep = [x for x in union if cnt[x] > 0]
+            for x in keep:
+                cnt[x] += 1
+            labs.append(keep)
+            dep.append(dep[a] or dep[b])
+            size = lambda ls: sum(l2[x] for x in ls if x not in S)
+            feats[i, 0] = size(labs[a]) + (lb if dep[a] else 0.0)
+            feats[i, 1] = size(labs[b]) + (lb if dep[b] else 0.0)
+            feats[i, 2] = size(keep) + (lb if dep[-1] else 0.0)
+            feats[i, 3] = sum(l2[x] for x in union if x not in keep and x not in S)
+            reps[i] = nbatch if dep[-1] else 1
+        return feats, reps
+
     def auto_batch(self, sliced_edges, budget_bytes=32 << 30, max_batch=1024):
         """Largest power-of-two batch of slices whose per-slice intermediates
         (three live at a time, at most) fit in ``budget_bytes``."""

@@ -105,6 +105,48 @@ def test_learned_plan_amplitudes_agree_with_flop_plan(pq, O, be):
     model.close()
 
 
+def test_sliced_features_and_slicing_set_ranking(pq, O, be):
+    """Sliced step features: with no slicing they are the plan's own; with
+    slicing the per-amplitude work they imply (runs x |C| K) equals the
+    unbatched steps once plus the batched ones per batch.  Ranking slicing
+    sets with the trained model picks a set whose sliced amplitude is the
+    state-vector amplitude."""
+    from pqgb300 import costmodel as CM
+
+    if not CM.WEIGHTS_FILE.exists():
+        pytest.skip("no trained weights committed yet")
+    r, c, d = 3, 4, 8
+    bits = "100110101100"
+    g = pq.random_grid_gates(r, c, d, seed=21)
+    net = pq.build_network(r * c, g, backend=be, decompose=True)
+    pq.add_input(net, "0" * (r * c))
+    pq.add_output(net, bits)
+    steps, cm, mx, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    p = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    f0, reps0 = p.sliced_features([], 4)
+    np.testing.assert_allclose(f0[:, :4], p.features()[:, :4])
+    assert np.all(reps0 == 1)
+    sl = p.choose_slices(max_sliced=4, log2_target=0)
+    f1, reps1 = p.sliced_features(sl, 4)
+    sizes = p.sliced_sizes(sl)
+    assert all((rp > 1) == b for rp, (_, b) in zip(reps1, sizes))
+    np.testing.assert_allclose(f1[:, 2], [sz + (2.0 if b else 0.0) for sz, b in sizes])
+    p.close()
+    model = CM.CostModel.load(be)
+    chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=4, slice_targets=(6, 4))
+    model.close()
+    assert "sliced" in chosen and np.isfinite(chosen["pred_us"])
+    pc = pq.NetworkPlan(net, steps=chosen["steps"], out_edges=[])
+    if chosen["sliced"]:
+        amp = pc.run_sliced(chosen["sliced"], batch=4)
+    else:
+        pc.execute()
+        amp = complex(np.asarray(pc.result()).reshape(-1)[0])
+    pc.close()
+    ref = O.statevector(r * c, g)[O.amplitude_index(bits)]
+    assert abs(amp - ref) / 2.0 ** -6 < 1e-6
+
+
 def test_trained_weights_file_loads(pq, be):
     from pqgb300 import costmodel as CM
 
