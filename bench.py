@@ -140,13 +140,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="grid6x6_d16_sliced",
-                    choices=["grid6x6_d16_sliced", "grid4x5_d12_amps", "grid7x7_d14_learned", "uneven512", "pair"],
+                    choices=["grid6x6_d16_sliced", "grid6x6_d16_accuracy", "grid4x5_d12_amps", "grid7x7_d14_learned",
+                             "uneven512", "pair"],
                     help="grid7x7_d14_learned: learned plan selection over sweep orders and 256 seeded greedy "
                          "orders for a 7x7 depth-14 single amplitude, end to end; pair: one pairwise contraction "
                          "of the dominant shape (M x K c64 boundary times K x N c128 gate-column tensor), for "
                          "kernel profiling")
     ap.add_argument("--candidates", type=int, default=256, help="seeded random-greedy orders ranked by the model")
     ap.add_argument("--circuits", type=int, default=512, help="circuits of the uneven512 workload")
+    ap.add_argument("--amplitudes", type=int, default=8, help="amplitudes of the grid6x6_d16_accuracy workload")
     ap.add_argument("--check", type=int, default=8, help="uneven512 circuits also run in complex128 for the error")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
@@ -173,7 +175,43 @@ def main():
         return run_learned(args)
     if args.workload == "uneven512":
         return run_uneven(args)
+    if args.workload == "grid6x6_d16_accuracy":
+        return run_accuracy(args)
     return run_gb300(args, world, rank)
+
+
+def run_accuracy(args):
+    """Error distribution of the headline configuration: ``--amplitudes``
+    single amplitudes of the 6x6 depth-16 circuit (bitstrings of ranks
+    0, 1, ...: the headline's is rank 0), each computed in ``--precision``
+    with the learned plan and in the plain complex-FP64 path with the
+    flop-count plan; reports every relative error and their rms and max."""
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    prec_name = args.precision if args.precision != "auto" else "ozaki"
+    prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
+    errs, scaled = [], []
+    for r in range(args.amplitudes):
+        w = build_sliced(pq, prec, args.rows, args.cols, args.depth, rank=r, target=args.slice_target)
+        a = w["plan"].run_sliced(w["sliced"], batch=w["plan"].auto_batch(w["sliced"]))
+        w["plan"].close()
+        w["be"].close()
+        w64 = build_sliced(pq, pq.PREC_C128, args.rows, args.cols, args.depth, rank=r, target=args.slice_target,
+                           planner="flop")
+        a64 = w64["plan"].run_sliced(w64["sliced"], batch=w64["plan"].auto_batch(w64["sliced"]))
+        w64["plan"].close()
+        w64["be"].close()
+        errs.append(abs(a - a64) / abs(a64))
+        scaled.append(abs(a - a64) / 2.0 ** (-(args.rows * args.cols) / 2))
+    line = {"workload": f"grid{args.rows}x{args.cols}_depth{args.depth}_sliced_accuracy", "precision": prec_name,
+            "metric": "relative amplitude error vs the plain complex-FP64 GPU path", "amplitudes": len(errs),
+            "rel_errors": errs, "rms": float(np.sqrt(np.mean(np.square(errs)))), "max": float(np.max(errs)),
+            "max_err_over_2^-n/2": float(np.max(scaled)), "target": 1e-6,
+            "plans": "learned plan (mixed) vs flop-count plan (FP64)", "data": "synthetic (seeded random circuit)"}
+    print(json.dumps(line))
+    return 0
 
 
 AMP_INDEX = "__amplitudes__"
