@@ -151,6 +151,8 @@ def main():
     ap.add_argument("--amplitudes", type=int, default=8, help="amplitudes of the grid6x6_d16_accuracy workload")
     ap.add_argument("--check", type=int, default=8, help="uneven512 circuits also run in complex128 for the error")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
+    ap.add_argument("--pair-order", default="mk", choices=["mk", "km"],
+                    help="memory order of the pair's A: contiguous along M (mk) or along K (km)")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
     ap.add_argument("--depth", type=int, default=16)
@@ -472,10 +474,12 @@ def run_pair(args):
     rng = np.random.default_rng(0)
     A = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))).astype(np.complex64)
     B = rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))
-    be.save_tensor_data("a", A)
+    km = args.pair_order == "km"
+    be.save_tensor_data("a", A.T if km else A)  # stored column-major: (K, M) has K contiguous
     be.save_tensor_data("b", B)
     h = C.c_void_p()
-    L.check(be.lib.pq_plan_create(be.ctx, 2, L.arr(C.c_int32, [2, 2]), L.arr(C.c_int32, [0, 1, 1, 2]), 3,
+    L.check(be.lib.pq_plan_create(be.ctx, 2, L.arr(C.c_int32, [2, 2]),
+                                  L.arr(C.c_int32, [1, 0, 1, 2] if km else [0, 1, 1, 2]), 3,
                                   L.arr(C.c_int64, [M, K, N]), 1, L.arr(C.c_int32, [0, 1]), 2,
                                   L.arr(C.c_int32, [0, 2]), C.byref(h)), be.ctx, "plan_create")
     ids = L.arr(C.c_int64, [be.id_of("a"), be.id_of("b")])
@@ -506,7 +510,8 @@ def run_pair(args):
     be.lib.pq_plan_destroy(h)
     be.close()
     ms = sum(times) / len(times)
-    print(json.dumps({"workload": "pair", "pair": {"M": M, "N": N, "K": K}, "precision": args.precision,
+    print(json.dumps({"workload": "pair", "pair": {"M": M, "N": N, "K": K, "a_order": args.pair_order},
+                      "precision": args.precision,
                       "ms_per_contraction": ms, "algorithmic_tflops": 8.0 * M * N * K / ms / 1e9,
                       "gpu_launches_per_contraction": launches / max(1, args.steps),
                       "max_abs_err_over_max_abs_vs_fp64": err, "l2": "flushed between steps (256 MiB write)"}))

@@ -40,7 +40,8 @@
 // for the 64 rows: 2 MMAs (M=128, N=TN, K=16) per slice pair and K tile.
 //
 // Kernels (one launch each, in stream order):
-//   k_oz_exp        row scale exponents of A, column scale exponents of B
+//   k_oz_exp        row scale exponents of A (k_oz_exp_k when A is contiguous
+//                   along K), column scale exponents of B
 //   k_oz_pack       B's slices into planes [z][col tile][k tile][plane][TN*16
 //                   bf16] in the canonical no-swizzle K-major UMMA layout
 //                   (8-row x 16-byte core matrices), planes {Re s0..s4, Im
@@ -53,12 +54,17 @@
 //                  16-deep K tile into the shared-memory ring;
 //     warp 1       TMEM owner and MMA issuer: 30 tcgen05.mma (kind::f16,
 //                  bf16) per K tile into three TN-column accumulators (levels
-//                  0, 1, 2-4);
+//                  0, 1, 2-4); narrow tiles (TN <= 64) alternate between two
+//                  such sets, so a tile's MMAs do not wait for the epilogue
+//                  of the one before;
 //     warps 2-9    A converters: gather A's 64 x 16 complex values of the K
-//                  tile through its index map straight from HBM (the next K
-//                  tile's loads in flight while this one is sliced), slice
+//                  tile through its index map straight from HBM (the group's
+//                  next K tile in flight while this one is sliced), slice
 //                  them and store the [Ar; Ai; -Ar] stacks into the ring (no
-//                  slice planes of A ever reach HBM);
+//                  slice planes of A ever reach HBM); for complex64 A two
+//                  groups of four warps take alternate K tiles, each thread
+//                  8 consecutive k of one row, so every store is a whole
+//                  16-byte core-matrix row;
 //     warps 10-17  epilogue, once per tile: Cr from TMEM lanes 0-63, Ci from
 //                  lanes 64-127; the levels are combined with an error-free
 //                  two-sum, scaled by 2^(ea+eb) and scattered through the
@@ -104,9 +110,12 @@ struct OzCfg {
   static constexpr uint32_t b_bytes = Sl<NSL>::planes * kBTile * 2;        // B planes of one K tile
   static constexpr uint32_t stage_bytes = NSL * kStackBytes + b_bytes;
   static constexpr int stages = (TN == 128 && NSL == 5) ? 3 : 4;
-  static constexpr uint32_t tmem_cols = TN == 128 ? 512 : (TN == 64 ? 256 : (TN == 32 ? 128 : 64));
+  // accumulator sets (three levels of TN columns each): two for TN <= 64, so
+  // that the MMAs of the next tile run while the epilogue drains this one
+  static constexpr int acc_sets = TN <= 64 ? 2 : 1;
+  static constexpr uint32_t tmem_cols = TN == 128 ? 512 : (TN == 64 ? 512 : (TN == 32 ? 256 : 128));
   static constexpr int cw = TN / 2;                                         // columns per epilogue warp
-  static_assert(3 * TN <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
+  static_assert(acc_sets * 3 * TN <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
 };
 
 // slice pairs, level 0 first, then level 1, then the higher levels (the
@@ -204,6 +213,73 @@ __global__ void __launch_bounds__(256) k_oz_exp(const T* __restrict__ X, const _
   }
 }
 
+// Row scale exponents of A when A is contiguous along K (its first K mode
+// has stride 1 and extent >= 2) but not along M: KL consecutive lanes read
+// consecutive k of one row (KL = the first K mode's extent, a power of two,
+// at most 32), combine their maxima with shuffles, and the RS = 32 / KL row
+// groups of a warp take consecutive rows -- when A's first M mode follows its
+// first K mode in memory, every load of a warp is one contiguous 256-byte
+// run.  A warp takes four such steps at a time, twice; one block of 8 warps
+// per 64 RS rows and batch index z.
+template <typename T>
+__global__ void __launch_bounds__(256) k_oz_exp_k(const T* __restrict__ X, const __grid_constant__ GemmDesc d,
+                                                  int64_t rows, int KL, int* __restrict__ e_out) {
+  using R = typename Real<T>::R;
+  __shared__ int64_t koff[kMaxK];
+  const int64_t z = blockIdx.y;
+  for (int t = threadIdx.x; t < d.K; t += blockDim.x) koff[t] = decode(t, d.nk, d.kdim, d.ksa);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int RS = 32 / KL;
+  const int sub = lane / KL, kl = lane % KL;
+  const int64_t zo = decode(z, d.nz, d.zdim, d.zsa);
+  const int64_t r0 = (int64_t)blockIdx.x * 64 * RS + warp * 8 * RS;
+#pragma unroll 1
+  for (int rr = 0; rr < 8 * RS; rr += 4 * RS) {
+    const T* xr[4];
+    bool v[4];
+    R mx[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t row = r0 + rr + i * RS + sub;
+      v[i] = row < rows;
+      xr[i] = X + zo + (v[i] ? decode(row, d.nm, d.mdim, d.msa) : 0);
+      mx[i] = 0;
+    }
+#pragma unroll 2
+    for (int k = kl; k < d.K; k += KL) {
+      const int64_t o = koff[k];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (v[i]) {
+          const T x = xr[i][o];
+          mx[i] = fmax(mx[i], absmax((R)x.x, (R)x.y));
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      for (int s = KL / 2; s > 0; s >>= 1) mx[i] = fmax(mx[i], __shfl_xor_sync(0xffffffffu, mx[i], s));
+      if (kl == 0 && v[i]) e_out[z * rows + r0 + rr + i * RS + sub] = exp_of(mx[i]);
+    }
+  }
+}
+
+// A's row exponents: the K-major kernel when A's first K mode has stride 1
+// (and its first M mode does not), else the row-per-thread kernel.
+template <typename T>
+void row_exponents(const T* A, const GemmDesc& d, int* ea, cudaStream_t s) {
+  int KL = 1;
+  if (d.nk > 0 && d.ksa[0] == 1 && !(d.nm > 0 && d.msa[0] == 1))
+    while (KL < 32 && 2 * KL <= d.kdim[0]) KL *= 2;
+  if (KL >= 2) {
+    const int64_t rows_per_block = 64 * (32 / KL);
+    k_oz_exp_k<T><<<dim3((unsigned)ceil_div(d.M, rows_per_block), (unsigned)d.Z), 256, 0, s>>>(A, d, d.M, KL, ea);
+  } else {
+    k_oz_exp<T, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, s>>>(A, d, 0, d.M, ea);
+  }
+}
+
 // The slices of x (|x| < 1 after scaling); every step is exact in R.
 template <typename R, int NSL>
 __device__ __forceinline__ void slices(R x, float* s) {
@@ -287,8 +363,8 @@ struct alignas(1024) OzSmem {
   int64_t koff[kMaxK];                                                        // A's K offsets
   uint64_t full[OzCfg<TN, NSL>::stages];
   uint64_t empty[OzCfg<TN, NSL>::stages];
-  uint64_t accf;
-  uint64_t acce;
+  uint64_t accf[2];  // accumulator set b holds a finished tile
+  uint64_t acce[2];  // the epilogue has read accumulator set b
   uint64_t drain;
   uint32_t tmem_base;
 };
@@ -316,6 +392,17 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 __device__ __forceinline__ void sts64(uint32_t addr, uint32_t a, uint32_t b) {
   asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
 }
+__device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+// A values per converter thread and K tile: 8 for complex64 A (whole 16-byte
+// core-matrix rows), 4 for complex128 A.
+constexpr int kConvThreads = 32 * kConvWarps;
+template <typename TA>
+__host__ __device__ constexpr int conv_values() {
+  return sizeof(TA) == 8 ? 8 : 4;
+}
 // Generic-proxy shared-memory writes made visible to the tensor core's reads.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -329,6 +416,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   constexpr int kSlices = NSL, kPlanes = Sl<NSL>::planes, kPairs = Sl<NSL>::pairs;
   constexpr int kStages = CF::stages;
   constexpr uint32_t kTmemCols = CF::tmem_cols;
+  constexpr int kSets = CF::acc_sets;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   OzSmem<TN, NSL>& sm = *reinterpret_cast<OzSmem<TN, NSL>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -336,11 +424,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&sm.full[s], 1 + kConvWarps);  // producer's expect_tx + one arrival per converter warp
+      // producer's expect_tx + one arrival per warp of the converter group of the K tile
+      mbar_init(&sm.full[s], 1 + kConvWarps * 4 / conv_values<TA>());
       mbar_init(&sm.empty[s], 1);
     }
-    mbar_init(&sm.accf, 1);
-    mbar_init(&sm.acce, kEpiWarps);  // one arrival per epilogue warp
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accf[b], 1);
+      mbar_init(&sm.acce[b], kEpiWarps);  // one arrival per epilogue warp
+    }
     mbar_init(&sm.drain, 1);
     mbar_init_fence();
   }
@@ -382,8 +473,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       int64_t g = 0;  // K tiles consumed so far
       int64_t t = 0;  // tiles of this CTA
       for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
-        // the epilogue of the previous tile has read the accumulators
-        if (!mbar_wait(&sm.acce, (uint32_t)((t & 1) ^ 1))) {
+        // the epilogue has read this accumulator set's previous tile
+        const int b = (int)(t % kSets);
+        if (!mbar_wait(&sm.acce[b], (uint32_t)(((t / kSets) & 1) ^ 1))) {
           ok = false;
           break;
         }
@@ -403,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int p = 0; p < kPairs; ++p) {
             const int i = pair_i<NSL>(p), j = pair_j<NSL>(p);
             const uint32_t acc = (kt == 0 && first_of_level(p)) ? 0u : 1u;
-            const uint32_t dl = tmem + (uint32_t)(level_of(p) * TN);
+            const uint32_t dl = tmem + (uint32_t)((b * 3 + level_of(p)) * TN);
             const uint64_t x1 = a0 + (uint64_t)((i * kStackBytes) >> 4);             // [Ar; Ai]
             const uint64_t x2 = a0 + (uint64_t)((i * kStackBytes + 8 * 128) >> 4);   // [Ai; -Ar]
             const uint64_t br = b0 + (uint64_t)(((0 * kSlices + j) * CF::kBTile * 2) >> 4);
@@ -414,61 +506,90 @@ __global__ void __launch_bounds__(kThreads, 1)
           mma_commit(&sm.empty[s]);  // smem stage free once these MMAs finish
         }
         if (!ok) break;
-        mma_commit(&sm.accf);  // tile accumulators ready for the epilogue
+        mma_commit(&sm.accf[b]);  // tile accumulators ready for the epilogue
       }
       // every MMA issued has finished once this arrives (TMEM is freed below)
       mma_commit(&sm.drain);
       if (!mbar_wait(&sm.drain, 0)) ok = false;
     }
   } else if (warp < 2 + kConvWarps) {
-    // converters: thread c handles row r = c % 64 and the 4 K values
-    // [4q, 4q+4) of every K tile (half of a 16-byte core-matrix row per
-    // stack block)
+    // converters: with NV values per thread and K tile, the converter warps
+    // form NV / 4 groups that take alternate K tiles; thread ch of a group
+    // handles row r = ch % 64 and the NV consecutive K values from
+    // kq = (ch / 64) NV of its K tiles.  Complex64 A: NV = 8, a whole 16-byte
+    // core-matrix row per stack block, stored without bank conflicts;
+    // complex128 A: NV = 4 (half rows; fewer registers), one group.
+    constexpr int NV = conv_values<TA>(), H = NV / 4, GT = kConvThreads / H;
     const int c = threadIdx.x - 64;
-    const int r = c & (kRows - 1), qd = c >> 6;
+    const int grp = c / GT, ch = c % GT;
+    const int r = ch & (kRows - 1), kq = (ch >> 6) * NV;
     using R = typename Real<TA>::R;
-    // byte offset of (slice 0, block 0, row r, K quarter qd) in the stacks
-    const uint32_t row_off = (uint32_t)((((qd >> 1) * 24 + (r >> 3)) * 8 + (r & 7)) * 16 + (qd & 1) * 8);
-    int64_t g = 0;
-    for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x) {
+    // byte offset of (slice 0, block 0, row r, K value kq) in the stacks
+    const uint32_t row_off = (uint32_t)((((kq >> 3) * 24 + (r >> 3)) * 8 + (r & 7)) * 16 + (kq & 7) * 2);
+    // This CTA's K tiles form one sequence g = tile number * ktiles + kt; the
+    // group takes g = grp, grp + H, ...  The next one's A values and row
+    // exponent are loaded while this one is sliced, across tile boundaries
+    // (a tile's rows and exponent are looked up once per tile).
+    const int64_t ntl = blockIdx.x < ntot ? (ntot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t items = ntl * ktiles;
+    int64_t ptl = -1;  // tile (number within this CTA) of the row below
+    const TA* prow = A;
+    bool pm = false;
+    int en = kExpZero;  // exponent of the prefetched K tile's row (a load in flight)
+    auto row_info = [&](int64_t tl) {
+      const int64_t tile = blockIdx.x + tl * gridDim.x;
       const int64_t rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
       const int64_t m = mt * kRows + r;
-      const bool mrow = m < d.M;
-      const int e = mrow ? ea[z * d.M + m] : kExpZero;
-      const bool live = mrow && e != kExpZero;
-      const float2 f = inv_scale(live ? e : 0);
-      const TA* arow = A + (live ? decode(z, d.nz, d.zdim, d.zsa) + decode(m, d.nm, d.mdim, d.msa) : 0);
-      auto load = [&](int64_t kt, TA* v) {
+      pm = m < d.M;
+      en = pm ? ea[z * d.M + m] : kExpZero;
+      prow = A + (pm ? decode(z, d.nz, d.zdim, d.zsa) + decode(m, d.nm, d.mdim, d.msa) : 0);
+      ptl = tl;
+    };
+    // zeros past the operand (and for rows outside it); an all-zero row's
+    // values are zeros themselves, whatever its exponent
+    auto load = [&](int64_t kt, TA* v) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int64_t k = kt * TK + qd * 4 + q;
-          if (live && k < d.K) {
-            v[q] = arow[sm.koff[k]];
-          } else {
-            v[q].x = 0;
-            v[q].y = 0;
-          }
+      for (int q = 0; q < NV; ++q) {
+        const int64_t k = kt * TK + kq + q;
+        if (pm && k < d.K) {
+          v[q] = prow[sm.koff[k]];
+        } else {
+          v[q].x = 0;
+          v[q].y = 0;
         }
-      };
-      TA nxt[4];
-      load(0, nxt);
-      for (int64_t kt = 0; kt < ktiles; ++kt, ++g) {
-        const int s = (int)(g % kStages);
-        const uint32_t ph = (uint32_t)((g / kStages) & 1);
-        TA cur[4];
+      }
+    };
+    TA nxt[NV];
+    if (grp < items) {
+      row_info(grp / ktiles);
+      load(grp % ktiles, nxt);
+    }
+    for (int64_t gk = grp; gk < items && ok; gk += H) {
+      const int e = en;
+      TA cur[NV];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
-        if (kt + 1 < ktiles) load(kt + 1, nxt);  // in flight while this tile is sliced
-        float re[kSlices][4], im[kSlices][4];
+      for (int q = 0; q < NV; ++q) cur[q] = nxt[q];
+      if (gk + H < items) {  // in flight while this K tile is sliced
+        const int64_t gp = gk + H, tl = gp / ktiles;
+        if (tl != ptl) row_info(tl);
+        load(gp - tl * ktiles, nxt);
+      }
+      const float2 f = inv_scale(e != kExpZero ? e : 0);
+      {
+        const int s = (int)(gk % kStages);
+        const uint32_t ph = (uint32_t)((gk / kStages) & 1);
+        uint32_t pr[kSlices][NV / 2], pim[kSlices][NV / 2];  // bf16 pairs (k, k + 1) of Ar, Ai
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float a[kSlices], b[kSlices];
-          slices<R, NSL>(scale_row((R)cur[q].x, e, f), a);
-          slices<R, NSL>(scale_row((R)cur[q].y, e, f), b);
+        for (int q = 0; q < NV; q += 2) {
+          float a0[kSlices], b0[kSlices], a1[kSlices], b1[kSlices];
+          slices<R, NSL>(scale_row((R)cur[q].x, e, f), a0);
+          slices<R, NSL>(scale_row((R)cur[q].y, e, f), b0);
+          slices<R, NSL>(scale_row((R)cur[q + 1].x, e, f), a1);
+          slices<R, NSL>(scale_row((R)cur[q + 1].y, e, f), b1);
 #pragma unroll
           for (int i = 0; i < kSlices; ++i) {
-            re[i][q] = a[i];
-            im[i][q] = b[i];
+            pr[i][q / 2] = pack_bf16x2(a0[i], a1[i]);
+            pim[i][q / 2] = pack_bf16x2(b0[i], b1[i]);
           }
         }
         bool got = mbar_wait(&sm.empty[s], ph ^ 1);
@@ -480,12 +601,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t base = smem_u32(sm.stage[s]) + row_off;
 #pragma unroll
         for (int i = 0; i < kSlices; ++i) {
-          const uint32_t r0 = pack_bf16x2(re[i][0], re[i][1]), r1 = pack_bf16x2(re[i][2], re[i][3]);
-          const uint32_t i0 = pack_bf16x2(im[i][0], im[i][1]), i1 = pack_bf16x2(im[i][2], im[i][3]);
           const uint32_t slice = base + (uint32_t)(i * kStackBytes);
-          sts64(slice, r0, r1);                                           // Ar
-          sts64(slice + 8 * 128, i0, i1);                                 // Ai
-          sts64(slice + 16 * 128, r0 ^ 0x80008000u, r1 ^ 0x80008000u);   // -Ar
+          constexpr uint32_t kNeg = 0x80008000u;
+          if constexpr (NV == 8) {
+            sts128(slice, pr[i][0], pr[i][1], pr[i][2], pr[i][3]);                              // Ar
+            sts128(slice + 8 * 128, pim[i][0], pim[i][1], pim[i][2], pim[i][3]);                // Ai
+            sts128(slice + 16 * 128, pr[i][0] ^ kNeg, pr[i][1] ^ kNeg, pr[i][2] ^ kNeg, pr[i][3] ^ kNeg);  // -Ar
+          } else {
+            sts64(slice, pr[i][0], pr[i][1]);                        // Ar
+            sts64(slice + 8 * 128, pim[i][0], pim[i][1]);            // Ai
+            sts64(slice + 16 * 128, pr[i][0] ^ kNeg, pr[i][1] ^ kNeg);  // -Ar
+          }
         }
         fence_proxy_async();
         __syncwarp();
@@ -504,26 +630,41 @@ __global__ void __launch_bounds__(kThreads, 1)
     R* Cr = reinterpret_cast<R*>(C);
     constexpr int PW = CW >= 16 ? 16 : 8;   // columns per TMEM load
     constexpr int NU = (CW + 31) / 32;       // columns of the warp's range per lane
-    int64_t t = 0;
-    for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
-      const int64_t nt = tile % ntiles, rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
-      // per-tile offsets and scales, loaded while the tile's MMAs run: the
-      // row's from this lane, the warp's columns spread over the lanes
-      const int64_t m = mt * kRows + r;
-      const bool mrow = m < d.M;
-      const int64_t base = mrow ? decode(z, d.nz, d.zdim, d.zsc) + cm_tab[m] : 0;
-      const int exa = mrow ? ea[z * d.M + m] : kExpZero;
-      const int64_t c0 = nt * TN + h * CW;
+    // per-tile offsets and scales, loaded one tile ahead: the row's from
+    // this lane, the warp's columns spread over the lanes
+    struct Meta {
+      int64_t base, c0;
+      int exa;
+      bool mrow;
       int ebl[NU];
       long long cnl[NU];
+    };
+    auto meta = [&](int64_t tile, Meta& M) {
+      const int64_t nt = tile % ntiles, rr = tile / ntiles, mt = rr % mtiles, z = rr / mtiles;
+      const int64_t m = mt * kRows + r;
+      M.mrow = m < d.M;
+      M.base = M.mrow ? decode(z, d.nz, d.zdim, d.zsc) + cm_tab[m] : 0;
+      M.exa = M.mrow ? ea[z * d.M + m] : kExpZero;
+      M.c0 = nt * TN + h * CW;
 #pragma unroll
       for (int u = 0; u < NU; ++u) {
-        const int64_t col = c0 + lane + 32 * u;
+        const int64_t col = M.c0 + lane + 32 * u;
         const bool valid = lane + 32 * u < CW && col < d.N;
-        ebl[u] = valid ? eb[z * d.N + col] : kExpZero;
-        cnl[u] = valid ? (long long)cn_tab[col] : 0;
+        M.ebl[u] = valid ? eb[z * d.N + col] : kExpZero;
+        M.cnl[u] = valid ? (long long)cn_tab[col] : 0;
       }
-      bool got = mbar_wait(&sm.accf, (uint32_t)(t & 1));
+    };
+    Meta nm;
+    if (blockIdx.x < ntot) meta(blockIdx.x, nm);
+    int64_t t = 0;
+    for (int64_t tile = blockIdx.x; tile < ntot && ok; tile += gridDim.x, ++t) {
+      const Meta M = nm;
+      if (tile + gridDim.x < ntot) meta(tile + gridDim.x, nm);  // in flight during this tile
+      const bool mrow = M.mrow;
+      const int64_t base = M.base, c0 = M.c0;
+      const int exa = M.exa;
+      const int b = (int)(t % kSets);
+      bool got = mbar_wait(&sm.accf[b], (uint32_t)((t / kSets) & 1));
       got = __all_sync(0xffffffffu, got);  // the TMEM loads below are warp-collective
       if (!got) {
         ok = false;
@@ -533,7 +674,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int piece = 0; piece < CW / PW; ++piece) {
         __syncwarp();  // the TMEM loads are warp-collective
-        const uint32_t col = (uint32_t)(h * CW + piece * PW);
+        const uint32_t col = (uint32_t)(b * 3 * TN + h * CW + piece * PW);
         float l0[PW], l1[PW], l2[PW];
         if constexpr (PW == 16) {
           tmem_ld16(lane_base + col + 0 * TN, l0);
@@ -548,13 +689,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (piece == CW / PW - 1) {  // every value of this tile is in registers
           fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&sm.acce);
+          if (lane == 0) mbar_arrive(&sm.acce[b]);
         }
 #pragma unroll
         for (int j = 0; j < PW; ++j) {
           const int cc = piece * PW + j;  // column within the warp's range
-          const int ebj = __shfl_sync(0xffffffffu, ebl[cc / 32], cc % 32);
-          const long long cnj = __shfl_sync(0xffffffffu, cnl[cc / 32], cc % 32);
+          const int ebj = __shfl_sync(0xffffffffu, M.ebl[cc / 32], cc % 32);
+          const long long cnj = __shfl_sync(0xffffffffu, M.cnl[cc / 32], cc % 32);
           if (mrow && c0 + cc < d.N) {
             const int ex = exa + ebj;
             const R v = (exa == kExpZero || ex < -2 * 1100) ? (R)0 : combine(l0[j], l1[j], l2[j], ex, R());
@@ -670,7 +811,11 @@ cudaError_t oz_gemm_tn(const void* A, const __nv_bfloat16* pb, void* C, const Ge
 
 bool eligible_oriented(const GemmDesc& d) {
   if (d.M < 64 || d.N < 8 || d.K < 16 || d.K > kMaxK) return false;
-  if (d.Z > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535 || ceil_div(d.M, 128) > 65535) return false;
+  // fewer than 512 complex products per output (e.g. a tall operand absorbing
+  // a 16-column gate tensor over K = 16): memory-bound work whose per-tile
+  // costs here exceed a plain FP32 pass, and whose FP32 sums have <= 32 terms
+  if (d.N * d.K < 512) return false;
+  if (d.Z > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535) return false;  // grid y / z of the B passes
   return layout(d, 5).total <= (size_t(24) << 30);
 }
 
@@ -689,11 +834,9 @@ static cudaError_t launch_oz_n(int ta, int tb, int tc, const void* A, const void
   auto* ea = (int*)(base + L.ea);
   auto* eb = (int*)(base + L.eb);
   if (ta == PQ_C128)
-    k_oz_exp<double2, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, stream>>>(
-        (const double2*)A, d, 0, d.M, ea);
+    row_exponents((const double2*)A, d, ea, stream);
   else
-    k_oz_exp<float2, 128><<<dim3((unsigned)ceil_div(d.M, 128), (unsigned)d.Z), 256, 0, stream>>>(
-        (const float2*)A, d, 0, d.M, ea);
+    row_exponents((const float2*)A, d, ea, stream);
   if (tb == PQ_C128)
     prep_b_tn<double2, NSL>(B, L.tn, pb, eb, d, L.nt, L.kt, stream);
   else

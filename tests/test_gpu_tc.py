@@ -205,9 +205,11 @@ def test_ozaki_matches_cpu_restatement(pq):
     assert np.all(np.abs(got - ref) <= ozaki_bound(A, B, ref))
 
 
-def test_ozaki_row_scales_and_zero_rows(pq):
+@pytest.mark.parametrize("order", ["mk", "km"])
+def test_ozaki_row_scales_and_zero_rows(pq, order):
     """Rows and columns of wildly different magnitude (per-row scaling), an
-    all-zero row of A and an all-zero column of B."""
+    all-zero row of A and an all-zero column of B; A contiguous along M (row
+    per thread exponent pass) or along K (row per warp)."""
     rng = np.random.default_rng(8)
     A = rand(rng, (300, 128)) * np.exp2(rng.integers(-60, 60, size=(300, 1)))
     B = rand(rng, (128, 100)) * np.exp2(rng.integers(-40, 40, size=(1, 100)))
@@ -215,7 +217,10 @@ def test_ozaki_row_scales_and_zero_rows(pq):
     B[:, 5] = 0
     A = A.astype(np.complex64)
     be = ozaki_backend(pq)
-    got, nl = run(be, A, [-1, 1], B.astype(np.complex64), [1, -2])
+    if order == "km":
+        got, nl = run(be, A.T, [1, -1], B.astype(np.complex64), [1, -2])
+    else:
+        got, nl = run(be, A, [-1, 1], B.astype(np.complex64), [1, -2])
     be.close()
     assert nl == OZ_LAUNCHES
     B = B.astype(np.complex64).astype(np.complex128)
@@ -275,3 +280,138 @@ def test_ozaki_k512_exact_limit(pq):
             assert np.all(np.abs(got - ref) <= ozaki_bound(A, B, ref))
         else:
             assert rel_err(got, ref) < TOL
+
+
+def _restatement_match(got, A, B):
+    """complex64 result vs the CPU restatement: within one ulp plus 2^-28 of
+    |row of A| |column of B|, bit-identical on most elements."""
+    from oracle import ozaki_oracle as Z
+
+    orc, _ = Z.ozaki_matmul(A, B)
+    na = np.sqrt(np.sum(np.abs(A) ** 2, axis=1))
+    nb = np.sqrt(np.sum(np.abs(B) ** 2, axis=0))
+    for part in (np.real, np.imag):
+        g, o = part(got).astype(np.float64), part(orc).astype(np.float64)
+        ulp = np.spacing(np.abs(o).astype(np.float32)).astype(np.float64)
+        assert np.all(np.abs(g - o) <= ulp + 2.0 ** -28 * np.outer(na, nb))
+        assert np.mean(g == o) > 0.95
+
+
+@pytest.mark.parametrize("order", ["mk", "km"])
+@pytest.mark.parametrize("n,k,small", [(16, 40, 0), (16, 256, 0), (32, 24, 0), (32, 72, 0), (48, 40, 0),
+                                       (64, 256, 0), (16, 48, 1 << 30)],
+                         ids=["n16-k40", "n16-k256", "n32-k24", "n32-k72", "n48-k40", "n64-k256", "n16-c128"])
+def test_ozaki_narrow_many_tiles_per_cta(pq, order, n, k, small):
+    """Narrow tiles (N <= 64: two accumulator sets in TMEM, alternate tiles)
+    over many row tiles: 64 * 152 * 3 + 37 rows give every persistent CTA
+    three or four tiles (the last one ragged), and with an odd number of K
+    tiles the two converter groups (alternate K tiles) swap roles from one
+    tile to the next; A contiguous along M or along K (the K-major exponent
+    pass), complex64 or complex128, with an all-zero row; a ragged last K
+    tile."""
+    rng = np.random.default_rng(n + k)
+    m = 64 * 152 * 3 + 37
+    A = rand(rng, (m, k))
+    A[1000] = 0
+    B = rand(rng, (k, n))
+    if not small:
+        A, B = A.astype(np.complex64), B.astype(np.complex64)
+    be = ozaki_backend(pq, small=small)
+    if order == "km":
+        got, nl = run(be, A.T, [1, -1], B, [1, -2])  # stored column-major: K contiguous
+    else:
+        got, nl = run(be, A, [-1, 1], B, [1, -2])
+    be.close()
+    assert nl == OZ_LAUNCHES
+    A, B = A.astype(np.complex128), B.astype(np.complex128)
+    ref = A @ B
+    assert np.all(got[1000] == 0)
+    assert np.all(np.abs(got - ref) <= ozaki_bound(A, B, ref))
+    if not small:
+        _restatement_match(got, A, B)
+
+
+def test_ozaki_narrow_tiles_across_batch(pq, O):
+    """A narrow batched pair (hyper mode z kept in the result): persistent
+    CTAs cross z boundaries as well as row tiles, three K tiles per tile."""
+    import ctypes as C
+    from pqgb300 import _lib as L
+
+    rng = np.random.default_rng(12)
+    m, k, n, z = 3000, 40, 16, 9
+    A = rand(rng, (m, k, z)).astype(np.complex64)
+    B = rand(rng, (k, n, z)).astype(np.complex64)
+    be = ozaki_backend(pq)
+    be.save_tensor_data("a", A)
+    be.save_tensor_data("b", B)
+    h = C.c_void_p()
+    rc = be.lib.pq_plan_create(be.ctx, 2, L.arr(C.c_int32, [3, 3]), L.arr(C.c_int32, [0, 1, 3, 1, 2, 3]), 4,
+                               L.arr(C.c_int64, [m, k, n, z]), 1, L.arr(C.c_int32, [0, 1]), 3,
+                               L.arr(C.c_int32, [3, 2, 0]), C.byref(h))
+    L.check(rc, be.ctx, "plan_create")
+    ids = L.arr(C.c_int64, [be.id_of("a"), be.id_of("b")])
+    n0 = be.launch_count()
+    L.check(be.lib.pq_plan_execute(h, ids, be.id_of("r")), be.ctx, "execute")
+    assert be.launch_count() - n0 == OZ_LAUNCHES
+    got = be.load_tensor_data("r")
+    be.lib.pq_plan_destroy(h)
+    be.close()
+    A, B = A.astype(np.complex128), B.astype(np.complex128)
+    for iz in range(z):
+        ref = A[:, :, iz] @ B[:, :, iz]
+        assert np.all(np.abs(got[iz].T - ref) <= ozaki_bound(A[:, :, iz], B[:, :, iz], ref))
+
+
+def test_3xbf16_narrow_many_tiles_per_cta(pq):
+    """Three bf16 slices on 16-wide tiles, two or three tiles per CTA."""
+    from oracle import ozaki_oracle as Z
+
+    rng = np.random.default_rng(13)
+    A = rand(rng, (64 * 152 * 2 + 5, 64)).astype(np.complex64)
+    B = rand(rng, (64, 16)).astype(np.complex64)
+    be = pq.GB300Backend(3, small_elems=0)
+    got, nl = run(be, A, [-1, 1], B, [1, -2])
+    be.close()
+    assert nl == OZ_LAUNCHES
+    A, B = A.astype(np.complex128), B.astype(np.complex128)
+    ref = A @ B
+    assert np.all(np.abs(got - ref) <= Z.error_bound(A, B, ref, n_slices=3))
+
+
+def test_ozaki_tall_narrow_pair(pq):
+    """More than 65535 * 128 rows (a 2^23-row boundary tensor absorbing a
+    16-column gate tensor over K = 32, stored contiguous along K): the exact
+    path takes it, the exponent pass on grid x with no 65535 limit."""
+    rng = np.random.default_rng(14)
+    m, k, n = (1 << 23) + 4097, 32, 16
+    A = rng.standard_normal((m, 2 * k), dtype=np.float32).view(np.complex64)
+    B = rand(rng, (k, n)).astype(np.complex64)
+    be = ozaki_backend(pq)
+    got, nl = run(be, A.T, [1, -1], B, [1, -2])  # A.T is (K, M) column-major: no host copy
+    be.close()
+    assert nl == OZ_LAUNCHES
+    rows = np.concatenate([np.arange(64), rng.choice(m, 4096, replace=False), np.arange(m - 64, m)])
+    A, B = A[rows].astype(np.complex128), B.astype(np.complex128)
+    ref = A @ B
+    assert np.all(np.abs(got[rows] - ref) <= ozaki_bound(A, B, ref))
+
+
+@pytest.mark.parametrize("ia", [[1, -1, -2, 2, -3, 3, -4, 4, -5, 5, -6, 6, -7, -8, -9, -10],
+                                [1, 2, -1, -2, 3, -3, 4, -4, 5, -5, 6, -6, -7, -8, -9, -10],
+                                [1, 2, 3, -1, -2, 4, -3, 5, -4, 6, -5, -6, -7, -8, -9, -10]],
+                         ids=["k-run-2", "k-run-4", "k-run-8"])
+def test_ozaki_stride1_mode_contracted(pq, O, ia):
+    """A's unit-stride mode is contracted, in a run of 2, 4 or 8 elements
+    before its first open mode (a boundary tensor whose fastest qubits meet
+    the gate tensor): the exponent pass reads A K-major with 2, 4 or 8 lanes
+    per row; all bond-2 modes, K = 64, M = 1024, N = 16."""
+    rng = np.random.default_rng(15 + len(ia))
+    ib = [1, 2, 3, 4, 5, 6, -11, -12, -13, -14]
+    A = (rand(rng, [2] * len(ia)) * np.exp2(rng.integers(-30, 30, size=[2] * len(ia)) // 8)).astype(np.complex64)
+    B = rand(rng, [2] * len(ib)).astype(np.complex64)
+    be = ozaki_backend(pq)
+    got, nl = run(be, A, ia, B, ib)
+    be.close()
+    assert nl == OZ_LAUNCHES
+    ref = O.contract_tensors_arrays(A.astype(np.complex128), ia, B.astype(np.complex128), ib)
+    assert rel_err(got, ref) < 3e-7
