@@ -391,15 +391,20 @@ def run_learned(args, rows=7, cols=7, depth=14):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     net = network(be)
+    t_net = time.perf_counter() - t0
     model = CM.CostModel.load(be)
     # orders and slicing sets ranked together (unsliced, and the slice
     # chooser at 2^target, 2^(target-2), 2^(target-4) elements)
+    phases = {}
     chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=args.candidates,
-                                               slice_targets=(target, target - 2, target - 4), batch=1024)
+                                               slice_targets=(target, target - 2, target - 4), batch=1024,
+                                               timings=phases)
     model.close()
+    t2 = time.perf_counter()
     plan = pq.NetworkPlan(net, steps=chosen["steps"], out_edges=[])
     sliced = chosen.get("sliced", [])
     t_plan = time.perf_counter() - t0
+    phases = {"network_s": t_net, **phases, "compile_plan_s": time.perf_counter() - t2}
     amp = amplitude(plan, sliced)
     t_e2e = time.perf_counter() - t0
     # steady state: the same plan again, inputs resident
@@ -435,7 +440,7 @@ def run_learned(args, rows=7, cols=7, depth=14):
             "depth": depth, "precision": prec_name,
             "metric": "end-to-end seconds to one amplitude (network -> plan -> amplitude)",
             "value": t_e2e, "unit": "s", "higher_is_better": False,
-            "planning_s": t_plan, "steady_amplitudes_per_s": len(ts) / sum(ts) if ts else None,
+            "planning_s": t_plan, "planning_phases_s": phases, "steady_amplitudes_per_s": len(ts) / sum(ts) if ts else None,
             "learned_plan": {"name": chosen["name"], "log2_cmacs": float(np.log2(chosen["cmacs"])),
                              "pred_us": chosen["pred_us"]},
             "flop_plan": {"name": best_flop["name"], "log2_cmacs": float(np.log2(best_flop["cmacs"])),

@@ -14,6 +14,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import time
 from pathlib import Path
 
 import numpy as np
@@ -264,7 +265,7 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
 
 
 def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_factor=8.0, max_elems=2**30,
-                 slice_targets=(), max_sliced=10, batch=1024):
+                 slice_targets=(), max_sliced=10, batch=1024, timings=None):
     """Rank candidate plans -- and, with ``slice_targets``, candidate slicing
     sets of each (the slice chooser at each target, log2 elements, for plans
     whose largest intermediate exceeds the largest target) -- by the model's
@@ -273,8 +274,11 @@ def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_facto
     multiply-adds (or above ``max_elems`` without slicing) are rejected, and
     the flop-optimal plan is the fallback.  Returns (chosen, flop-optimal
     plan, all candidates); each candidate carries ``pred_us`` and, when
-    slicing sets were ranked, its best ``sliced`` edge list."""
+    slicing sets were ranked, its best ``sliced`` edge list.  ``timings``, a
+    dict, receives the seconds spent generating and ranking candidates."""
+    t0 = time.perf_counter()
     cands, out_edges = candidate_plans(network, out_edges, n_random, seed)
+    t1 = time.perf_counter()
     best_flop = min(cands, key=lambda c: (c["cmacs"], c["max_elems"]))
     for c in cands:
         if c["cmacs"] > flop_factor * best_flop["cmacs"] or (c["max_elems"] > max_elems and not slice_targets):
@@ -303,4 +307,7 @@ def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_facto
     chosen = min(cands, key=lambda c: c["pred_us"])
     if not np.isfinite(chosen["pred_us"]):
         chosen = best_flop
+    if timings is not None:
+        timings["candidates_s"] = t1 - t0
+        timings["ranking_s"] = time.perf_counter() - t1
     return chosen, best_flop, cands

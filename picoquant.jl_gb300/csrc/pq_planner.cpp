@@ -42,6 +42,46 @@ double l2size_of(const std::vector<int>& l, const std::vector<double>& l2dim) {
   return s;
 }
 
+// Candidate pairs with their energies: a dense array (uniform sampling and
+// swap-removal), a key -> slot index, and the same pairs ordered by energy
+// (minimum, ties, and the exact sampling window).
+struct CandSet {
+  std::vector<uint64_t> keys;
+  std::vector<double> en;
+  std::unordered_map<uint64_t, int> slot;
+  std::set<std::pair<double, uint64_t>> order;
+  static uint64_t key(int u, int v) {
+    const int a = std::min(u, v), b = std::max(u, v);
+    return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+  }
+  void set(uint64_t k, double e) {
+    auto it = slot.find(k);
+    if (it != slot.end()) {
+      order.erase({en[it->second], k});
+      en[it->second] = e;
+    } else {
+      slot.emplace(k, (int)keys.size());
+      keys.push_back(k);
+      en.push_back(e);
+    }
+    order.insert({e, k});
+  }
+  void erase(uint64_t k) {
+    auto it = slot.find(k);
+    if (it == slot.end()) return;
+    const int i = it->second, last = (int)keys.size() - 1;
+    order.erase({en[i], k});
+    if (i != last) {
+      keys[i] = keys[last];
+      en[i] = en[last];
+      slot[keys[i]] = i;
+    }
+    keys.pop_back();
+    en.pop_back();
+    slot.erase(it);
+  }
+};
+
 Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, const std::vector<double>& l2dim,
                   const std::vector<int>& out_labels, double alpha, double tau, std::mt19937_64& rng) {
   const int nl = n_leaves;
@@ -52,6 +92,8 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
   std::vector<char> live(nv, 0);
   std::vector<int> cnt(nlab, 0);
   std::vector<std::vector<int>> holders(nlab);  // live values per label (lazy)
+  std::vector<uint32_t> stamp(nlab, 0);         // label marks for set intersections
+  uint32_t cur_stamp = 0;
   for (int i = 0; i < nl; ++i) {
     lab[i] = leaves[i];
     l2[i] = l2size_of(lab[i], l2dim);
@@ -63,49 +105,41 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
   }
   for (int x : out_labels) cnt[x]++;
   Trial t;
-  // candidate pairs (a < b) that share a label, with their energies, and the
-  // same pairs ordered by energy: the minimum and the pairs near it (the
-  // only ones with a weight that matters) are read from the front
-  using Key = std::pair<int, int>;
-  std::map<Key, double> cand;
-  std::set<std::pair<double, Key>> order;
-  auto result_labels = [&](int a, int b, std::vector<int>& r, double& l2c, double& l2all) {
-    r.clear();
+  CandSet cs;
+  // labels of the result of (a, b) -- a's kept labels in a's order, then b's
+  // labels not in a -- with log2 of its size and of the size of every label
+  // involved; O(|a| + |b|) with the label stamps
+  auto result_labels = [&](int a, int b, std::vector<int>* r, double& l2c, double& l2all) {
+    if (r) r->clear();
+    l2c = 0;
     l2all = 0;
+    ++cur_stamp;
+    for (int x : lab[b]) stamp[x] = cur_stamp;
     for (int x : lab[a]) {
       l2all += l2dim[x];
-      int c = cnt[x] - 1;
-      if (std::find(lab[b].begin(), lab[b].end(), x) != lab[b].end()) c--;
-      if (c > 0) r.push_back(x);
+      const bool in_b = stamp[x] == cur_stamp;
+      if (cnt[x] - 1 - (in_b ? 1 : 0) > 0) {
+        l2c += l2dim[x];
+        if (r) r->push_back(x);
+      }
+      if (in_b) stamp[x] = cur_stamp - 1;  // seen: skipped in b's pass
     }
     for (int x : lab[b]) {
-      if (std::find(lab[a].begin(), lab[a].end(), x) != lab[a].end()) continue;
+      if (stamp[x] != cur_stamp) continue;  // also in a
       l2all += l2dim[x];
-      if (cnt[x] - 1 > 0) r.push_back(x);
+      if (cnt[x] - 1 > 0) {
+        l2c += l2dim[x];
+        if (r) r->push_back(x);
+      }
     }
-    l2c = l2size_of(r, l2dim);
+    ++cur_stamp;  // a's marks (cur_stamp - 2 after this) never match again
   };
-  std::vector<int> tmp;
   auto score = [&](int a, int b) {
     double l2c, l2all;
-    result_labels(a, b, tmp, l2c, l2all);
+    result_labels(a, b, nullptr, l2c, l2all);
     return std::exp2(l2c) - alpha * (std::exp2(l2[a]) + std::exp2(l2[b]));
   };
-  auto set_score = [&](int u, int v) {
-    const Key k(std::min(u, v), std::max(u, v));
-    auto it = cand.find(k);
-    if (it != cand.end()) order.erase({it->second, k});
-    const double e = score(k.first, k.second);
-    cand[k] = e;
-    order.insert({e, k});
-  };
-  auto erase_key = [&](int u, int v) {
-    const Key k(std::min(u, v), std::max(u, v));
-    auto it = cand.find(k);
-    if (it == cand.end()) return;
-    order.erase({it->second, k});
-    cand.erase(it);
-  };
+  auto set_score = [&](int u, int v) { cs.set(CandSet::key(u, v), score(u, v)); };
   // live values sharing a label with v
   auto partners = [&](int v, std::vector<int>& nb) {
     nb.clear();
@@ -115,7 +149,7 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
     std::sort(nb.begin(), nb.end());
     nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
   };
-  std::vector<int> nb, nb2;
+  std::vector<int> nb, nb2, hyper;
   for (int i = 0; i < nl; ++i) {
     partners(i, nb);
     for (int u : nb)
@@ -124,38 +158,49 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
   int next = nl;
   int nlive = nl;
   std::uniform_real_distribution<double> U(0.0, 1.0);
-  std::vector<Key> keys;
+  std::vector<uint64_t> keys;
   std::vector<double> w;
+  auto split = [](uint64_t k, int& a, int& b) {
+    a = (int)(k >> 32);
+    b = (int)(k & 0xffffffffu);
+  };
+  std::vector<int> r;
   while (nlive > 1) {
     int a = -1, b = -1;
-    if (!order.empty()) {
-      const double emin = order.begin()->first;
+    if (!cs.order.empty()) {
+      const double emin = cs.order.begin()->first;
       keys.clear();
       if (tau <= 0) {
         // deterministic greedy with random tie-break
-        for (auto it = order.begin(); it != order.end() && it->first <= emin; ++it) keys.push_back(it->second);
-        auto k = keys[std::uniform_int_distribution<size_t>(0, keys.size() - 1)(rng)];
-        a = k.first;
-        b = k.second;
+        for (auto it = cs.order.begin(); it != cs.order.end() && it->first <= emin; ++it) keys.push_back(it->second);
+        split(keys[std::uniform_int_distribution<size_t>(0, keys.size() - 1)(rng)], a, b);
       } else {
-        // weights exp(-(e - emin) / T); pairs beyond 50 T weigh < e^-50
+        // weights exp(-(e - emin) / T): a uniform pick accepted with its
+        // weight (at most 64 tries), else the exact draw over the pairs
+        // within 50 T of the minimum (beyond it weights are below e^-50)
         const double T = tau * std::max(1.0, std::fabs(emin));
-        w.clear();
-        double tot = 0;
-        for (auto it = order.begin(); it != order.end() && it->first - emin <= 50.0 * T; ++it) {
-          const double x = std::exp(-(it->first - emin) / T);
-          keys.push_back(it->second);
-          w.push_back(x);
-          tot += x;
+        std::uniform_int_distribution<size_t> pick(0, cs.keys.size() - 1);
+        for (int tries = 0; tries < 64 && a < 0; ++tries) {
+          const size_t i = pick(rng);
+          if (U(rng) < std::exp(-(cs.en[i] - emin) / T)) split(cs.keys[i], a, b);
         }
-        double r = U(rng) * tot;
-        size_t k = 0;
-        for (; k + 1 < w.size(); ++k) {
-          r -= w[k];
-          if (r <= 0) break;
+        if (a < 0) {
+          w.clear();
+          double tot = 0;
+          for (auto it = cs.order.begin(); it != cs.order.end() && it->first - emin <= 50.0 * T; ++it) {
+            const double x = std::exp(-(it->first - emin) / T);
+            keys.push_back(it->second);
+            w.push_back(x);
+            tot += x;
+          }
+          double u = U(rng) * tot;
+          size_t k = 0;
+          for (; k + 1 < w.size(); ++k) {
+            u -= w[k];
+            if (u <= 0) break;
+          }
+          split(keys[k], a, b);
         }
-        a = keys[k].first;
-        b = keys[k].second;
       }
     } else {
       // disjoint pieces: outer product of the two smallest
@@ -173,21 +218,29 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
       b = std::max(s1, s2);
     }
     double l2c, l2all;
-    std::vector<int> r;
-    result_labels(a, b, r, l2c, l2all);
+    result_labels(a, b, &r, l2c, l2all);
     t.cmacs += std::exp2(l2all);
     t.max_l2 = std::max(t.max_l2, l2c);
     t.steps.push_back(a);
     t.steps.push_back(b);
+    // labels held by both and kept (hyper-indices): their counts drop, so
+    // the pairs of their other holders are rescored below; no other pair's
+    // energy changes
+    hyper.clear();
+    ++cur_stamp;
+    for (int x : lab[b]) stamp[x] = cur_stamp;
+    for (int x : lab[a])
+      if (stamp[x] == cur_stamp && cnt[x] - 2 > 0) hyper.push_back(x);
+    ++cur_stamp;
     // retire a, b and every candidate pair that holds one of them
     partners(a, nb);
-    for (int u : nb) erase_key(a, u);
+    for (int u : nb) cs.erase(CandSet::key(a, u));
     partners(b, nb);
-    for (int u : nb) erase_key(b, u);
+    for (int u : nb) cs.erase(CandSet::key(b, u));
     live[a] = live[b] = 0;
     for (int x : lab[a]) cnt[x]--;
     for (int x : lab[b]) cnt[x]--;
-    int v = next++;
+    const int v = next++;
     lab[v] = r;
     l2[v] = l2c;
     live[v] = 1;
@@ -198,14 +251,14 @@ Trial greedy_once(int n_leaves, const std::vector<std::vector<int>>& leaves, con
       h.push_back(v);
     }
     nlive--;
-    // the counts of v's labels changed: every pair of a live value holding
-    // one of them is rescored, then v's own pairs are added
+    for (int x : hyper)
+      for (int u : holders[x]) {
+        if (u == v || !live[u]) continue;
+        partners(u, nb2);
+        for (int y : nb2)
+          if (y != v) set_score(u, y);
+      }
     partners(v, nb);
-    for (int u : nb) {
-      partners(u, nb2);
-      for (int x : nb2)
-        if (x != v) set_score(u, x);
-    }
     for (int u : nb) set_score(v, u);
   }
   return t;

@@ -472,44 +472,69 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
         glabels[q] = ls
     # labels internal to a group disappear; the group tensor keeps labels that
     # leave the group or are outputs
-    ext = {}
+    ngroups: dict[int, int] = {}
     for q in qs:
-        inner = {x for x in glabels[q] if sum(1 for p in qs if x in glabels[p]) > 1 or x in outset}
-        ext[q] = inner
+        for x in glabels[q]:
+            ngroups[x] = ngroups.get(x, 0) + 1
+    ext = {q: {x for x in glabels[q] if ngroups[x] > 1 or x in outset} for q in qs}
     l2 = [float(np.log2(d)) for d in dims]
-    adj = {q: set() for q in qs}
+    owners: dict[int, list] = {}
     for q in qs:
-        for p in qs:
-            if p != q and ext[q] & ext[p]:
-                adj[q].add(p)
-
-    def boundary_l2(absorbed_labels, absorbed):
-        # labels of the boundary: those of absorbed groups still needed outside
-        tot = 0.0
-        for x in absorbed_labels:
-            if x in outset or any(x in ext[p] for p in qs if p not in absorbed):
-                tot += l2[x]
-        return tot
+        for x in ext[q]:
+            owners.setdefault(x, []).append(q)
+    adj = {q: set() for q in qs}
+    for x, ow in owners.items():
+        for q in ow:
+            adj[q].update(p for p in ow if p != q)
 
     def greedy_order(start):
+        # the boundary after absorbing a set of groups: the labels of absorbed
+        # groups still held by an unabsorbed group or open; rem[x] counts the
+        # unabsorbed groups holding x, so one candidate's boundary is the
+        # current one plus a change over its own labels
+        rem = {x: len(ow) for x, ow in owners.items()}
+        bnd: set = set()
+        cur = 0.0
+
+        def absorb(c):
+            nonlocal cur
+            for x in ext[c]:
+                rem[x] -= 1
+                if x in bnd:
+                    if rem[x] == 0 and x not in outset:
+                        bnd.discard(x)
+                        cur -= l2[x]
+                elif rem[x] > 0 or x in outset:
+                    bnd.add(x)
+                    cur += l2[x]
+
+        def after(c):
+            d = 0.0
+            for x in ext[c]:
+                if x in bnd:
+                    if rem[x] == 1 and x not in outset:
+                        d -= l2[x]
+                elif rem[x] > 1 or x in outset:
+                    d += l2[x]
+            return cur + d
+
         order = [start]
         absorbed = {start}
-        labels = set(ext[start])
+        absorb(start)
+        front = set(adj[start])
         while len(order) < len(qs):
-            cands = set()
-            for q in order:
-                cands |= adj[q]
-            cands -= absorbed
+            cands = front - absorbed
             if not cands:
                 cands = set(qs) - absorbed
             best, bl = None, None
             for c in sorted(cands):
-                b = boundary_l2(labels | ext[c], absorbed | {c})
+                b = after(c)
                 if bl is None or b < bl - 1e-9:
                     best, bl = c, b
             order.append(best)
             absorbed.add(best)
-            labels |= ext[best]
+            absorb(best)
+            front |= adj[best]
         return order
 
     orders = [list(qs), list(reversed(qs))]
