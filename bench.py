@@ -867,7 +867,7 @@ OZ_GEMM_TRAFFIC_RATIO = 1.032 / 1.025
 def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks, prec_name=None):
     """Dominant kernel class by device time; achieved algorithmic FLOP/s or
     bytes/s of that class over its measured launch time."""
-    names = {0: "generic", 1: "gemm_simt", 2: "tcgen05", 3: "copy"}
+    names = {0: "generic", 1: "gemm_simt", 2: "tcgen05", 3: "copy", 4: "skinny"}
     info = {}
     for t, b, f in zip(ms, batched, feats):
         k = int(f[6])

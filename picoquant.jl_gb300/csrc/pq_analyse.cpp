@@ -244,6 +244,8 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
        precision == PQ_PREC_3XBF16) &&
       tc_eligible(precision, G))
     out.kclass = KC_TC;
+  else if (k_both && skinny_eligible(G))
+    out.kclass = KC_SKINNY;
   else if (gemm_shape || (k_both && out.ksize > kGenericKTab && G.M >= 8 && G.N >= 8))
     out.kclass = KC_GEMM;
   else

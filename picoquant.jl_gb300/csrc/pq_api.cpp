@@ -428,6 +428,9 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
   } else if (pp.kclass == KC_GEMM) {
     e = launch_gemm(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
     ctx->launches += 1;
+  } else if (pp.kclass == KC_SKINNY) {
+    e = launch_skinny(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.m, ctx->stream);
+    ctx->launches += 1;
   } else {
     e = launch_generic(A.dtype, B.dtype, C.dtype, A.ptr, B.ptr, C.ptr, pp.g, ctx->stream);
     ctx->launches += 1;

@@ -47,7 +47,12 @@ struct GemmDesc {
   int64_t zdim[kMaxModes], zsa[kMaxModes], zsb[kMaxModes], zsc[kMaxModes];
 };
 
-enum KernelClass : int { KC_GENERIC = 0, KC_GEMM = 1, KC_TC = 2, KC_COPY = 3 };
+enum KernelClass : int { KC_GENERIC = 0, KC_GEMM = 1, KC_TC = 2, KC_COPY = 3, KC_SKINNY = 4 };
+// Skinny pairs (pq_skinny.cu): a large operand (>= kSkinnyMinRows rows over
+// its free modes) against a small one, K <= kSkinnyK, the small side's free
+// extent <= kSkinnyN, no batch modes.
+constexpr int kSkinnyK = 16, kSkinnyN = 16;
+constexpr int64_t kSkinnyMinRows = 4096;
 // SIMT GEMM tile shapes: 64x64, 256x16 (narrow N), 16x256 (narrow M).
 enum GemmShape : int { GEMM_SQUARE = 0, GEMM_TALL = 1, GEMM_WIDE = 2 };
 struct GemmDesc;
@@ -126,13 +131,16 @@ int cuda_fail(Ctx* ctx, cudaError_t e, const char* what);
 int dev_alloc(Ctx* ctx, size_t bytes, void** p);
 void dev_free(Ctx* ctx, void* p, size_t bytes);
 
-// ---- kernel launchers (pq_kernels.cu, pq_gemm.cu) -------------------------
+// ---- kernel launchers (pq_kernels.cu, pq_gemm.cu, pq_skinny.cu) -----------
 // Element types are PQ_C64 / PQ_C128 per operand.  All launches are
 // asynchronous on `stream` and return the launch error.
 cudaError_t launch_generic(int ta, int tb, int tc, const void* A, const void* B, void* C,
                            const GenericDesc& d, cudaStream_t stream);
 cudaError_t launch_gemm(int ta, int tb, int tc, const void* A, const void* B, void* C,
                         const GemmDesc& d, cudaStream_t stream);
+bool skinny_eligible(const GemmDesc& d);
+cudaError_t launch_skinny(int ta, int tb, int tc, const void* A, const void* B, void* C,
+                          const GemmDesc& d, cudaStream_t stream);
 // out[c] = in[base + sum_i idx_i * stride_i] over `d` (uses csa as input
 // strides, C storage column-major), converting tin -> tout.
 cudaError_t launch_permute(int tin, int tout, const void* in, int64_t base, void* out,

@@ -64,6 +64,7 @@ int pq_measure_pairs(pq_ctx* c, int n_pairs, const int32_t* a_ranks, const int32
       if (q.kclass == KC_TC)
         return launch_tc(ctx->precision, ta[p], tb[p], tc[p], A, B, C, q.m, S, smax, ctx->d_status, ctx->stream);
       if (q.kclass == KC_GEMM) return launch_gemm(ta[p], tb[p], tc[p], A, B, C, q.m, ctx->stream);
+      if (q.kclass == KC_SKINNY) return launch_skinny(ta[p], tb[p], tc[p], A, B, C, q.m, ctx->stream);
       return launch_generic(ta[p], tb[p], tc[p], A, B, C, q.g, ctx->stream);
     };
     for (int p = 0; p < n_pairs && e == cudaSuccess; ++p) {

@@ -325,6 +325,8 @@ cudaError_t run_step(pq_plan* p, const Step& s, const void* A, const void* B, vo
                        ctx->d_status, ctx->stream);
     case KC_GEMM:
       return launch_gemm(s.ta, s.tb, s.tc, A, B, C, s.pp.m, ctx->stream);
+    case KC_SKINNY:
+      return launch_skinny(s.ta, s.tb, s.tc, A, B, C, s.pp.m, ctx->stream);
     default:
       return launch_generic(s.ta, s.tb, s.tc, A, B, C, s.pp.g, ctx->stream);
   }
