@@ -244,9 +244,9 @@ def run_uneven(args):
     """Batched uneven workload: ``--circuits`` seeded random grid circuits
     (qubits uniform in 12..30, grid factorised from the count, depth uniform
     in 8..24), 64 random-bitstring amplitudes each.  Per circuit the cheaper
-    of two strategies by a roofline estimate: the state vector (single-qubit
-    gates fused into two-qubit gates, gate-by-gate order, the 64 amplitudes
-    gathered) or the qubit-sweep tensor-network order with the 64 output
+    of two strategies by a roofline estimate: the state vector (gates fused
+    into blocks of at most four qubits, one pass over the state per block, the
+    64 amplitudes gathered) or the qubit-sweep tensor-network order with the 64 output
     bitstrings as one batch index.  Every plan is compiled, captured as a CUDA
     graph and launched from it; a step contracts all circuits.  The first
     ``--check`` circuits are also run in complex128 for the error."""
@@ -266,7 +266,7 @@ def run_uneven(args):
     for i, (n, d) in enumerate(specs):
         r, c = CI.grid_shape(n)
         gates = pq.random_grid_gates(r, c, d, seed=10_000 + i)
-        fused = CI.fuse_single_qubit_gates(gates)
+        fused = CI.fuse_gates(gates, 4)
         bits = pq.random_bitstrings(n, 64, seed=20_000 + i)
         t_sv = (2.0 ** n) * 16 * len(fused) / 6e12 + len(fused) * 4e-6
         host = _HostStore()

@@ -117,6 +117,67 @@ def fuse_single_qubit_gates(gates):
     return out
 
 
+def _apply_on(B, U, qs, block):
+    """U (on ``qs``, the first listed qubit the low bit) times the operator B
+    on ``block`` (first qubit the low bit): B's row bits are the tensor axes
+    of a C-order reshape, axis a holding bit m - 1 - a."""
+    m, k = len(block), len(qs)
+    T = B.reshape((2,) * m + (B.shape[1],))
+    Ut = np.asarray(U, dtype=np.complex128).reshape((2,) * (2 * k))
+    tgt = [m - 1 - block.index(qs[j]) for j in reversed(range(k))]
+    R = np.tensordot(Ut, T, axes=(list(range(k, 2 * k)), tgt))
+    return np.moveaxis(R, list(range(k)), tgt).reshape(B.shape)
+
+
+def fuse_gates(gates, max_qubits=4):
+    """The same circuit as blocks of at most ``max_qubits`` qubits (operator
+    convention of ``operator_to_tensor``), so that a state-vector order sweeps
+    the state once per block.  Greedy in circuit order: a gate joins the block
+    that is the latest on each of its qubits when that block has room; when
+    its qubits' latest blocks differ, those blocks are merged with it if each
+    is still the latest on all of its own qubits (so it can move past every
+    block in between, which acts on other qubits) and the union fits; else
+    the gate starts a block.  Exact: only commuting blocks are reordered."""
+    blocks = []   # [qubits (first = low bit), matrix, alive]
+    last = {}     # qubit -> index of its latest block
+    for U, qs in gates:
+        qs = list(qs)
+        U = np.asarray(U, dtype=np.complex128)
+        owners = sorted({last[q] for q in qs if q in last})
+        target = None
+        if len(owners) == 1:
+            b = owners[0]
+            if len(set(blocks[b][0]) | set(qs)) <= max_qubits:
+                target = b
+        elif len(owners) > 1:
+            union = set(qs)
+            for b in owners:
+                union |= set(blocks[b][0])
+            if len(union) <= max_qubits and all(last[q] == b for b in owners for q in blocks[b][0]):
+                qubits, M = [], np.ones((1, 1), dtype=np.complex128)
+                for b in owners:  # disjoint blocks: the later one's bits above
+                    qubits += blocks[b][0]
+                    M = np.kron(blocks[b][1], M)
+                    blocks[b][2] = False
+                blocks.append([qubits, M, True])
+                target = len(blocks) - 1
+                for q in qubits:
+                    last[q] = target
+        if target is None:
+            blocks.append([list(qs), U.copy(), True])
+            target = len(blocks) - 1
+        else:
+            blk = blocks[target]
+            for q in qs:
+                if q not in blk[0]:
+                    blk[0].append(q)  # a new highest bit
+                    blk[1] = np.kron(np.eye(2, dtype=np.complex128), blk[1])
+            blk[1] = _apply_on(blk[1], U, qs, blk[0])
+        for q in qs:
+            last[q] = target
+    return [(M, qubits) for qubits, M, alive in blocks if alive]
+
+
 def grid_shape(n_qubits):
     """Most square rows x cols factorisation of a qubit count (rows <= cols)."""
     best = (1, n_qubits)

@@ -165,3 +165,25 @@ def test_statevector_circuit_amplitudes(pq, O):
     plan.close()
     be.close()
     assert rel_err(got, O.statevector(n, gates)) < 2e-6
+
+
+def test_block_fused_statevector(pq, O):
+    """A 16-qubit circuit fused into blocks of at most four qubits, applied
+    block by block (16 x 16 skinny pairs), matches the oracle's state vector
+    of the unfused circuit."""
+    from pqgb300 import circuits as CI
+
+    n = 16
+    gates = pq.random_grid_gates(4, 4, 10, seed=23)
+    blocks = CI.fuse_gates(gates, 4)
+    be = pq.GB300Backend(1)
+    net = pq.build_network(n, blocks, backend=be)
+    pq.add_input(net, "0" * n)
+    plan = pq.NetworkPlan(net, steps=pq.planning.statevector_steps(net))
+    f = plan.features()
+    assert np.sum((f[:, 6] == KC_SKINNY) & (f[:, 3] == 4.0)) > 0  # 4-qubit blocks: K = 16
+    plan.execute()
+    got = plan.result().reshape(-1, order="F")
+    plan.close()
+    be.close()
+    assert rel_err(got, O.statevector(n, gates)) < 2e-6

@@ -176,6 +176,45 @@ def test_fused_gates_statevector_order(pq, O, host_backend):
     assert np.max(np.abs(out - O.statevector(6, gates))) < 1e-13
 
 
+@pytest.mark.parametrize("max_qubits", [2, 3, 4])
+def test_block_fused_gates(pq, O, host_backend, max_qubits):
+    """Gates fused into blocks of at most 2, 3 or 4 qubits (open blocks merged
+    when a gate joins them): exact, fewer blocks than gates, and the block
+    circuit contracted gate by gate on the host backend gives the original
+    circuit's state vector."""
+    from pqgb300 import circuits as CI
+
+    gates = pq.random_grid_gates(3, 3, 8, seed=11)
+    blocks = CI.fuse_gates(gates, max_qubits)
+    assert max(len(q) for _, q in blocks) <= max_qubits
+    assert len(blocks) < len(CI.fuse_single_qubit_gates(gates)) or max_qubits == 2
+    ref = O.statevector(9, gates)
+    assert np.max(np.abs(O.statevector(9, blocks) - ref)) < 1e-12
+    net = pq.build_network(9, blocks, backend=host_backend)
+    pq.add_input(net, "0" * 9)
+    pq.contract_network(net, pq.steps_to_pairs(net, pq.planning.statevector_steps(net)))
+    out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
+    assert np.max(np.abs(out - ref)) < 1e-12
+
+
+def test_block_fusion_keeps_order_of_random_gates(pq, O):
+    """Random gates of one to three qubits on arbitrary qubits: blocks of up
+    to four qubits reproduce the state vector (only commuting blocks move)."""
+    from pqgb300 import circuits as CI
+
+    rng = np.random.default_rng(3)
+    for _ in range(10):
+        gates = []
+        for _ in range(40):
+            k = int(rng.integers(1, 4))
+            qs = [int(q) for q in rng.choice(np.arange(1, 8), k, replace=False)]
+            z = rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k))
+            gates.append((np.linalg.qr(z)[0], qs))
+        ref = O.statevector(7, gates)
+        for m in (3, 4):
+            assert np.max(np.abs(O.statevector(7, CI.fuse_gates(gates, m)) - ref)) < 1e-12
+
+
 def test_batched_output_amplitudes(pq, O, host_backend):
     """Output tensors sharing one bitstring-batch index: one contraction of
     the sweep order gives the amplitudes of all bitstrings."""
