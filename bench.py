@@ -550,7 +550,9 @@ def workload_config(args, rows, cols, depth):
                 "plan": "learned cost model over qubit-sweep orders (flop-count planner judges; plain FP64 "
                         "path uses the flop-count plan)", "l2": "flushed between steps (256 MiB write)"}
     return {"workload": f"grid{rows}x{cols}_depth{depth}_1024_amplitudes", "qubits": rows * cols, "depth": depth,
-            "amplitudes_per_step": 1024, "plan": "flop-count planner (open outputs + gather)",
+            "amplitudes_per_step": 1024,
+            "plan": "flop-count planner over the circuit fused into blocks of up to four qubits (open outputs + "
+                    "gather)",
             "l2": "flushed between steps (256 MiB write)"}
 
 
@@ -703,13 +705,18 @@ def run_gb300(args, world, rank):
 
         amps_per_step = 1
     else:
+        from pqgb300 import circuits as CI
+
         rows, cols, depth = 4, 5, 12
         n = rows * cols
         gates = pq.random_grid_gates(rows, cols, depth, seed=2024)
         be = pq.GB300Backend(precision)
-        net = pq.build_network(n, gates, backend=be)
+        # the circuit as blocks of up to four qubits (exact): one pass over the
+        # state per block in a state-vector order
+        net = pq.build_network(n, CI.fuse_gates(gates, 4), backend=be)
         pq.add_input(net, "0" * n)
-        steps_, cm, mx, name = pq.planning.best_flop_plan(net, trials=4)
+        steps_, cm, mx, name = pq.planning.best_flop_plan(
+            net, trials=4, candidates=("sweep", "greedy", "wavefunction", "statevector"))
         plan = pq.NetworkPlan(net, steps=steps_)
         plan.capture()
         bits = pq.random_bitstrings(n, 1024, seed=7)

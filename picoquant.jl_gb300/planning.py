@@ -560,7 +560,8 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
 
 def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("sweep", "greedy", "wavefunction")):
     """The flop-count planner: the cheapest (complex multiply-adds) of the
-    candidate plans.  Returns (steps, cmacs, max_elems, name)."""
+    candidate plans ("sweep", "greedy", "wavefunction" and the gate-by-gate
+    "statevector" order).  Returns (steps, cmacs, max_elems, name)."""
     if out_edges is None:
         out_edges = open_output_edges(network)
     nodes, ranks, flat, dims, label_of = _leaf_arrays(network, out_edges)
@@ -578,6 +579,9 @@ def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("swee
             found.append((s, *plan_cost(ranks, flat, dims, s, outl), "wavefunction"))
         except KeyError:
             pass
+    if "statevector" in candidates and all(network.edges[e].src is not None for e in network.input_qubits):
+        s = statevector_steps(network, nodes)
+        found.append((s, *plan_cost(ranks, flat, dims, s, outl), "statevector"))
     return min(found, key=lambda t: (t[1], t[2]))
 
 

@@ -187,3 +187,28 @@ def test_block_fused_statevector(pq, O):
     plan.close()
     be.close()
     assert rel_err(got, O.statevector(n, gates)) < 2e-6
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["c64", "c128"])
+def test_block_fused_amplitudes_4x5(pq, O, prec):
+    """The 4x5 depth-12 circuit fused into blocks of up to four qubits, the
+    flop-count planner choosing among sweep, greedy, full-wavefunction and
+    state-vector orders: 1024 amplitudes gathered from the open-output result
+    match the oracle's state vector of the unfused circuit."""
+    from pqgb300 import circuits as CI
+
+    n = 20
+    gates = pq.random_grid_gates(4, 5, 12, seed=2024)
+    be = pq.GB300Backend(prec)
+    net = pq.build_network(n, CI.fuse_gates(gates, 4), backend=be)
+    pq.add_input(net, "0" * n)
+    steps, _, _, name = pq.planning.best_flop_plan(
+        net, trials=2, candidates=("sweep", "greedy", "wavefunction", "statevector"))
+    plan = pq.NetworkPlan(net, steps=steps)
+    bits = pq.random_bitstrings(n, 1024, seed=7)
+    got = np.asarray(plan.amplitudes(bits))
+    plan.close()
+    be.close()
+    ref = O.statevector(n, gates)[[O.amplitude_index(b) for b in bits]]
+    scale = np.sqrt(np.mean(np.abs(ref) ** 2))
+    assert np.max(np.abs(got - ref)) / scale < (2e-5 if prec == 1 else 1e-11)
