@@ -138,6 +138,19 @@ cudaError_t launch_generic(int ta, int tb, int tc, const void* A, const void* B,
                            const GenericDesc& d, cudaStream_t stream);
 cudaError_t launch_gemm(int ta, int tb, int tc, const void* A, const void* B, void* C,
                         const GemmDesc& d, cudaStream_t stream);
+// Up to kGroupMax independent small generic steps (complex128 operands and
+// result, K <= kGroupK) in one launch; member m runs on blocks
+// [blk[m], blk[m+1]) with descriptor descs[desc[m]] (device table).
+constexpr int kGroupMax = 64, kGroupK = 256;
+struct GenericGroup {
+  int n;
+  int blk[kGroupMax + 1];
+  int desc[kGroupMax];
+  const void* A[kGroupMax];
+  const void* B[kGroupMax];
+  void* C[kGroupMax];
+};
+cudaError_t launch_generic_group(const GenericGroup& g, const GenericDesc* d_descs, cudaStream_t stream);
 bool skinny_eligible(const GemmDesc& d);
 cudaError_t launch_skinny(int ta, int tb, int tc, const void* A, const void* B, void* C,
                           const GemmDesc& d, cudaStream_t stream);

@@ -159,6 +159,59 @@ cudaError_t launch_generic(int ta, int tb, int tc, const void* A, const void* B,
   return cudaGetLastError();
 }
 
+// Grouped small steps: one launch runs up to kGroupMax independent small
+// contractions (complex128 operands and results, K <= kGroupK), each on its
+// own range of blocks.  A block finds its member in the prefix table, copies
+// the member's descriptor (prepared once per plan) into shared memory and
+// runs the generic kernel's loop on it.
+__global__ void __launch_bounds__(kGenThreads)
+    k_generic_group(const __grid_constant__ GenericGroup g, const GenericDesc* __restrict__ descs) {
+  __shared__ GenericDesc sd;
+  __shared__ int64_t ka[kGroupK];
+  __shared__ int64_t kb[kGroupK];
+  int m = 0;
+  while (m + 1 < g.n && g.blk[m + 1] <= (int)blockIdx.x) ++m;
+  {
+    const int* src = reinterpret_cast<const int*>(descs + g.desc[m]);
+    int* dst = reinterpret_cast<int*>(&sd);
+    for (int t = threadIdx.x; t < (int)(sizeof(GenericDesc) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+  const int KT = (int)sd.ksize;
+  for (int k = threadIdx.x; k < KT; k += blockDim.x) {
+    int64_t x, y;
+    if (sd.pow2)
+      decodek<true>(k, sd, x, y);
+    else
+      decodek<false>(k, sd, x, y);
+    ka[k] = x;
+    kb[k] = y;
+  }
+  __syncthreads();
+  const double2* A = static_cast<const double2*>(g.A[m]);
+  const double2* B = static_cast<const double2*>(g.B[m]);
+  double2* C = static_cast<double2*>(g.C[m]);
+  const int64_t nb = g.blk[m + 1] - g.blk[m];
+  const int64_t step = nb * blockDim.x;
+  for (int64_t c = (int64_t)(blockIdx.x - g.blk[m]) * blockDim.x + threadIdx.x; c < sd.csize; c += step) {
+    int64_t oa, ob;
+    if (sd.pow2)
+      decode2<true>(c, sd, oa, ob);
+    else
+      decode2<false>(c, sd, oa, ob);
+    double2 acc = make_double2(0.0, 0.0);
+    KahanC ks;
+    dot_chunk(acc, ks, A + oa, B + ob, ka, kb, KT);
+    C[c] = acc;
+  }
+}
+
+cudaError_t launch_generic_group(const GenericGroup& g, const GenericDesc* d_descs, cudaStream_t stream) {
+  if (g.n <= 0 || g.blk[g.n] <= 0) return cudaSuccess;
+  k_generic_group<<<g.blk[g.n], kGenThreads, 0, stream>>>(g, d_descs);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Data movement
 // ---------------------------------------------------------------------------

@@ -38,6 +38,7 @@ struct Step {
   bool batched = false;
   bool is_copy = false;  // single-leaf network: result = permuted copy of x
   int ta = PQ_C128, tb = PQ_C128, tc = PQ_C128;  // storage types of A, B, C
+  int group = -1;        // launch group of small steps (consecutive steps share it)
 };
 
 struct Compiled {
@@ -53,7 +54,81 @@ struct Compiled {
   double cmacs = 0;
   int64_t max_elems = 0;
   int64_t launches = 0;
+  std::vector<GenericDesc> gdesc;  // descriptors of grouped steps (uploaded per plan)
+  std::vector<int> gdesc_of;       // per step: index into gdesc, or -1
 };
+
+// Small steps: complex128 generic contractions of at most kGroupSmall result
+// elements and K <= kGroupK.  They are launch-bound one by one.
+constexpr int64_t kGroupSmall = 1 << 16;
+
+bool groupable(const Step& s) {
+  return !s.is_copy && s.y >= 0 && s.pp.kclass == KC_GENERIC && s.ta == PQ_C128 && s.tb == PQ_C128 &&
+         s.tc == PQ_C128 && s.pp.csize >= 1 && s.pp.csize <= kGroupSmall && s.pp.g.ksize <= kGroupK;
+}
+
+// Launch groups: every maximal run of consecutive small steps (same batched
+// flag) is reordered by dependency level within the run -- a step's level is
+// one more than the highest level of a producer inside the run -- and each
+// level becomes one launch of up to kGroupMax steps (the per-qubit chains of
+// a circuit advance together).  Steps outside runs keep their positions, so
+// every step still follows its producers.
+void form_groups(Compiled& cp) {
+  const int n = (int)cp.steps.size();
+  std::vector<int> prod(cp.labels.size(), -1);
+  for (int i = 0; i < n; ++i) prod[cp.nleaves + cp.order[i]] = i;
+  std::vector<Step> steps;
+  std::vector<int> order;
+  steps.reserve(n);
+  order.reserve(n);
+  int gid = 0;
+  for (int i = 0; i < n;) {
+    if (!groupable(cp.steps[i])) {
+      steps.push_back(cp.steps[i]);
+      order.push_back(cp.order[i]);
+      ++i;
+      continue;
+    }
+    int j = i;
+    while (j < n && groupable(cp.steps[j]) && cp.steps[j].batched == cp.steps[i].batched) ++j;
+    std::vector<int> lvl(j - i, 0);
+    for (int t = i; t < j; ++t) {
+      int L = 0;
+      for (int v : {cp.steps[t].x, cp.steps[t].y}) {
+        if (v < 0) continue;
+        const int pi = prod[v];
+        if (pi >= i && pi < t) L = std::max(L, lvl[pi - i] + 1);
+      }
+      lvl[t - i] = L;
+    }
+    std::vector<int> idx(j - i);
+    for (int t = 0; t < j - i; ++t) idx[t] = t;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lvl[a] < lvl[b]; });
+    for (size_t a = 0; a < idx.size();) {
+      size_t b = a;
+      while (b < idx.size() && lvl[idx[b]] == lvl[idx[a]] && b - a < (size_t)kGroupMax) ++b;
+      const bool grp = b - a >= 2;
+      for (size_t c = a; c < b; ++c) {
+        Step st = cp.steps[i + idx[c]];
+        st.group = grp ? gid : -1;
+        steps.push_back(st);
+        order.push_back(cp.order[i + idx[c]]);
+      }
+      if (grp) ++gid;
+      a = b;
+    }
+    i = j;
+  }
+  cp.steps.swap(steps);
+  cp.order.swap(order);
+  cp.gdesc.clear();
+  cp.gdesc_of.assign(cp.steps.size(), -1);
+  for (size_t k = 0; k < cp.steps.size(); ++k)
+    if (cp.steps[k].group >= 0) {
+      cp.gdesc_of[k] = (int)cp.gdesc.size();
+      cp.gdesc.push_back(cp.steps[k].pp.g);
+    }
+}
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -97,17 +172,27 @@ void assign_arena(Compiled& cp, const std::vector<char>& pinned) {
     }
   };
   std::vector<size_t> voff(nv, 0), vsz(nv, 0);
-  for (int i = 0; i < (int)cp.steps.size(); ++i) {
-    Step& s = cp.steps[i];
-    int r = cp.nleaves + cp.order[i];
-    size_t sz = align_up(std::max<size_t>(s.bytes, 16), 256);
-    s.off = take(sz);
-    voff[r] = s.off;
-    vsz[r] = sz;
-    for (int v : {s.x, s.y}) {
-      if (v < cp.nleaves || v < 0) continue;
-      if (last_use[v] == i && !pinned[v] && v != cp.result_ssa) give(voff[v], vsz[v]);
+  // a launch group runs concurrently: all its results are placed before any
+  // of its inputs is released
+  const int n = (int)cp.steps.size();
+  for (int i = 0; i < n;) {
+    int j = i + 1;
+    if (cp.steps[i].group >= 0)
+      while (j < n && cp.steps[j].group == cp.steps[i].group) ++j;
+    for (int t = i; t < j; ++t) {
+      Step& s = cp.steps[t];
+      const int r = cp.nleaves + cp.order[t];
+      const size_t sz = align_up(std::max<size_t>(s.bytes, 16), 256);
+      s.off = take(sz);
+      voff[r] = s.off;
+      vsz[r] = sz;
     }
+    for (int t = i; t < j; ++t)
+      for (int v : {cp.steps[t].x, cp.steps[t].y}) {
+        if (v < cp.nleaves || v < 0) continue;
+        if (last_use[v] == t && !pinned[v] && v != cp.result_ssa) give(voff[v], vsz[v]);
+      }
+    i = j;
   }
   cp.arena_bytes = top;
 }
@@ -128,6 +213,11 @@ struct pq_plan {
   size_t arena_cap = 0;
   void* scratch = nullptr;
   size_t scratch_cap = 0;
+  // device tables of the grouped steps' descriptors (cp, scp)
+  void* d_gdesc = nullptr;
+  size_t d_gdesc_bytes = 0;
+  void* d_sgdesc = nullptr;
+  size_t d_sgdesc_bytes = 0;
   // graph
   cudaGraphExec_t gexec = nullptr;
   std::vector<const void*> graph_ptrs;
@@ -299,6 +389,13 @@ bool compile(const Ctx* ctx, const std::vector<std::vector<int>>& leaf_labels,
     cp.max_elems = std::max(cp.max_elems, p.csize);
     cp.launches += (p.kclass == KC_TC) ? tc_launch_count(ctx->precision, p.m) : 1;
   }
+  form_groups(cp);
+  cp.launches = 0;
+  for (size_t i = 0; i < cp.steps.size(); ++i) {
+    const Step& s = cp.steps[i];
+    if (s.group >= 0 && i > 0 && cp.steps[i - 1].group == s.group) continue;  // one launch per group
+    cp.launches += (s.pp.kclass == KC_TC) ? tc_launch_count(ctx->precision, s.pp.m) : 1;
+  }
   size_t sb = 0;
   for (auto& s : cp.steps)
     if (s.pp.kclass == KC_TC) sb = std::max(sb, tc_scratch_bytes(precision, s.pp.m));
@@ -396,16 +493,58 @@ int launch_all(pq_plan* p, const Compiled& cp, const std::vector<const void*>& l
   Ctx* ctx = p->ctx;
   std::vector<const void*> vptr;
   resolve(p, cp, leaf_ptrs, vptr);
-  for (size_t i = 0; i < cp.steps.size(); ++i) {
+  const GenericDesc* dd = (const GenericDesc*)(&cp == &p->scp ? p->d_sgdesc : p->d_gdesc);
+  const size_t n = cp.steps.size();
+  for (size_t i = 0; i < n; ++i) {
     const Step& s = cp.steps[i];
     if (only_batched && !s.batched) continue;
     if (only_unbatched && s.batched) continue;
+    if (s.group >= 0 && dd) {
+      GenericGroup g;
+      g.n = 0;
+      int blocks = 0;
+      size_t j = i;
+      for (; j < n && cp.steps[j].group == s.group; ++j) {
+        const Step& t = cp.steps[j];
+        g.blk[g.n] = blocks;
+        g.desc[g.n] = cp.gdesc_of[j];
+        g.A[g.n] = vptr[t.x];
+        g.B[g.n] = vptr[t.y];
+        g.C[g.n] = (char*)p->arena + t.off;
+        blocks += (int)std::min<int64_t>((t.pp.csize + 255) / 256, 64);
+        g.n++;
+      }
+      g.blk[g.n] = blocks;
+      ctx->launches += 1;
+      cudaError_t e = launch_generic_group(g, dd, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "plan group launch");
+      i = j - 1;
+      continue;
+    }
     const void* A = vptr[s.x];
     const void* B = s.y >= 0 ? vptr[s.y] : nullptr;
     void* C = (char*)p->arena + s.off;
     cudaError_t e = run_step(p, s, A, B, C);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "plan step launch");
   }
+  return PQ_OK;
+}
+
+// Copy a compiled plan's grouped-step descriptors to the device (once per
+// compile, outside any stream capture).
+int upload_groups(pq_plan* p, const Compiled& c, void** buf, size_t* bytes) {
+  Ctx* ctx = p->ctx;
+  if (*buf) dev_free(ctx, *buf, *bytes);
+  *buf = nullptr;
+  *bytes = 0;
+  if (c.gdesc.empty()) return PQ_OK;
+  const size_t b = c.gdesc.size() * sizeof(GenericDesc);
+  int st = dev_alloc(ctx, b, buf);
+  if (st) return st;
+  *bytes = b;
+  cudaError_t e = cudaMemcpyAsync(*buf, c.gdesc.data(), b, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "plan descriptor upload");
   return PQ_OK;
 }
 
@@ -482,6 +621,11 @@ int pq_plan_create(pq_ctx* c, int n_leaves, const int32_t* leaf_ranks, const int
     delete p;
     return fail(ctx, PQ_ERR_INVALID, "plan_create: " + err);
   }
+  const int st = upload_groups(p, p->cp, &p->d_gdesc, &p->d_gdesc_bytes);
+  if (st) {
+    delete p;
+    return st;
+  }
   *out = p;
   return PQ_OK;
 }
@@ -494,6 +638,8 @@ int pq_plan_destroy(pq_plan* p) {
   if (p->arena) dev_free(ctx, p->arena, p->arena_cap);
   if (p->scratch) dev_free(ctx, p->scratch, p->scratch_cap);
   if (p->d_acc) dev_free(ctx, p->d_acc, (size_t)p->out_elems * 32);
+  if (p->d_gdesc) dev_free(ctx, p->d_gdesc, p->d_gdesc_bytes);
+  if (p->d_sgdesc) dev_free(ctx, p->d_sgdesc, p->d_sgdesc_bytes);
   delete p;
   return PQ_OK;
 }
@@ -709,6 +855,8 @@ int prepare_sliced(pq_plan* p, const int64_t* leaf_ids, int n_sliced, const int3
     std::string err;
     if (!compile(ctx, ll, ldims, p->steps_in, outl, order, &bl, p->scp, err, &p->cp.dt))
       return fail(ctx, PQ_ERR_INVALID, "run_sliced: " + err);
+    const int su = upload_groups(p, p->scp, &p->d_sgdesc, &p->d_sgdesc_bytes);
+    if (su) return su;
     // gathered leaf buffers after the arena
     size_t off = align_up(p->scp.arena_bytes, 256);
     for (size_t j = 0; j < p->sl_leaf_desc.size(); ++j) {

@@ -205,3 +205,38 @@ def test_plan_rejects_bad_input(pq):
     assert e.value.code == L.PQ_ERR_INVALID
     plan.close()
     be.close()
+
+
+@pytest.mark.parametrize("prec", [0, 5], ids=["c128", "ozaki"])
+def test_small_steps_launch_in_groups(pq, O, prec):
+    """The qubit-sweep plan of a 4x4 depth-10 single amplitude: its per-qubit
+    chains are runs of small complex128 steps, launched level by level in
+    groups (fewer launches than steps, counted both at compile time and by
+    the context); the amplitude matches the state vector, directly, replayed
+    from a CUDA graph, and through the sliced path."""
+    be = pq.GB300Backend(prec)
+    n, bits = 16, "0110100111001010"
+    g = pq.random_grid_gates(4, 4, 10, seed=31)
+    net = pq.build_network(n, g, backend=be, decompose=True)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    steps, _, _, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    info = plan.info()
+    assert info["launches"] < info["steps"] // 2
+    n0 = be.launch_count()
+    plan.execute()
+    assert be.launch_count() - n0 == info["launches"]
+    ref = O.statevector(n, g)[O.amplitude_index(bits)]
+    tol = 1e-12 if prec == 0 else 1e-6
+    amp = complex(np.asarray(plan.result()).reshape(-1)[0])
+    assert abs(amp - ref) / 2.0 ** (-n / 2) < tol
+    plan.capture()
+    plan.execute()
+    assert complex(np.asarray(plan.result()).reshape(-1)[0]) == amp
+    sliced = plan.choose_slices(max_sliced=3, log2_target=8)
+    for batch in (1, 8):
+        a2 = plan.run_sliced(sliced, batch=batch)
+        assert abs(a2 - ref) / 2.0 ** (-n / 2) < tol
+    plan.close()
+    be.close()
