@@ -240,3 +240,53 @@ def test_small_steps_launch_in_groups(pq, O, prec):
         assert abs(a2 - ref) / 2.0 ** (-n / 2) < tol
     plan.close()
     be.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["c128", "c64"])
+def test_small_step_groups_chunked(pq, prec):
+    """65 independent 4 x 4 matrix products on the first level (one group of
+    64 and a single step), then a chain of 64 dependent products: the plan
+    result is the product of all 130 matrices."""
+    import ctypes as C
+
+    from pqgb300 import _lib as L
+
+    rng = np.random.default_rng(41)
+    npairs = 65
+    be = pq.GB300Backend(prec)
+    # labels: x_i = i (0..65), k_i = 66 + i
+    ranks, flat, ids, mats = [], [], [], []
+    for i in range(npairs):
+        A = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
+        B = rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))
+        for nm, M, lab in ((f"a{i}", A, [i, 66 + i]), (f"b{i}", B, [66 + i, i + 1])):
+            be.save_tensor_data(nm, M)
+            ranks.append(2)
+            flat += lab
+            ids.append(be.id_of(nm))
+        mats.append(A @ B)
+    dims = [4] * (66 + npairs)
+    steps = []
+    for i in range(npairs):
+        steps += [2 * i, 2 * i + 1]  # value 2*npairs + i = A_i B_i
+    v = 2 * npairs
+    nxt = 3 * npairs
+    for i in range(1, npairs):
+        steps += [v, 2 * npairs + i]
+        v = nxt
+        nxt += 1
+    h = C.c_void_p()
+    L.check(be.lib.pq_plan_create(be.ctx, len(ranks), L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
+                                  L.arr(C.c_int64, dims), len(steps) // 2, L.arr(C.c_int32, steps), 2,
+                                  L.arr(C.c_int32, [0, npairs]), C.byref(h)), be.ctx, "plan_create")
+    cm, mx, ar, la = C.c_double(), C.c_int64(), C.c_int64(), C.c_int64()
+    L.check(be.lib.pq_plan_info(h, C.byref(cm), C.byref(mx), C.byref(ar), C.byref(la)), be.ctx, "info")
+    assert la.value == 2 + (npairs - 1)  # the first level in two launches, then the chain
+    L.check(be.lib.pq_plan_execute(h, L.arr(C.c_int64, ids), be.id_of("r")), be.ctx, "execute")
+    got = be.load_tensor_data("r")
+    be.lib.pq_plan_destroy(h)
+    be.close()
+    ref = mats[0]
+    for M in mats[1:]:
+        ref = ref @ M
+    assert rel(got, ref) < TOL[prec]
