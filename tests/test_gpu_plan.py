@@ -290,3 +290,55 @@ def test_small_step_groups_chunked(pq, prec):
     for M in mats[1:]:
         ref = ref @ M
     assert rel(got, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["c128", "c64"])
+def test_small_step_groups_mixed_extents(pq, O, prec):
+    """Independent small steps with extents 3, 5, 6 and 7 (the grouped
+    kernel's division decode), three chains advancing together, then joined:
+    the plan result is the oracle's contraction."""
+    import ctypes as C
+
+    from pqgb300 import _lib as L
+
+    rng = np.random.default_rng(43)
+    ext = [3, 5, 6, 7, 2, 3, 5, 7, 6]
+    # chains c = 0, 1, 2: T_c0 [a_c, k_c] x T_c1 [k_c, m_c] x T_c2 [m_c, b_c]; then joined over b_c -> a_c's open
+    labels = {}
+    def lab(name, d):
+        if name not in labels:
+            labels[name] = (len(labels), d)
+        return labels[name][0]
+    leaves, ranks, flat, ids = [], [], [], []
+    be = pq.GB300Backend(prec)
+    for c in range(3):
+        a, k, m, b = ext[3 * c], ext[3 * c + 1], ext[3 * c + 2], 4
+        shapes = [((a, k), [f"a{c}", f"k{c}"]), ((k, m), [f"k{c}", f"m{c}"]), ((m, b), [f"m{c}", "b"])]
+        for t, (shp, names) in enumerate(shapes):
+            T = rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
+            nm = f"t{c}{t}"
+            be.save_tensor_data(nm, T)
+            leaves.append((T, names))
+            ranks.append(2)
+            flat += [lab(x, d) for x, d in zip(names, shp)]
+            ids.append(be.id_of(nm))
+    dims = [d for _, d in sorted(labels.values())]
+    # chain steps first (level 0: t_c0 t_c1 for each c; level 1: with t_c2), then the joins over "b"
+    steps = []
+    for c in range(3):
+        steps += [3 * c, 3 * c + 1]          # value 9 + c
+    for c in range(3):
+        steps += [9 + c, 3 * c + 2]          # value 12 + c: [a_c, b]
+    steps += [12, 13, 15, 14]                # value 15: [a0, b, a1] (b still open for chain 2), value 16
+    out = [labels["a0"][0], labels["a1"][0], labels["a2"][0]]
+    h = C.c_void_p()
+    L.check(be.lib.pq_plan_create(be.ctx, len(ranks), L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
+                                  L.arr(C.c_int64, dims), len(steps) // 2, L.arr(C.c_int32, steps), len(out),
+                                  L.arr(C.c_int32, out), C.byref(h)), be.ctx, "plan_create")
+    L.check(be.lib.pq_plan_execute(h, L.arr(C.c_int64, ids), be.id_of("r")), be.ctx, "execute")
+    got = be.load_tensor_data("r")
+    be.lib.pq_plan_destroy(h)
+    be.close()
+    T = [x[0] for x in leaves]
+    ref = np.einsum("ak,km,mb,cl,ln,nb,dp,pq,qb->acd", *T)
+    assert rel(got, ref) < TOL[prec]
