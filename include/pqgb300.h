@@ -274,6 +274,14 @@ int pq_plan_greedy_many(int n_leaves, const int32_t* leaf_ranks, const int32_t* 
                         int n_labels, const int64_t* label_dims, int n_out, const int32_t* out_labels,
                         double alpha, double tau, int n_draws, uint64_t seed, int n_threads,
                         int32_t* steps, double* cmacs, int64_t* max_elems);
+/* Cost of SSA steps (no reference counterpart: the flop-count planner's
+ * measure of a given order, src/backends.jl:30-41): complex multiply-adds
+ * summed over the steps and the largest intermediate (elements), with the
+ * executor's label rule (a label is summed once no other live tensor and no
+ * output carries it).  Host only. */
+int pq_plan_cost(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                 const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
+                 const int32_t* out_labels, double* cmacs, double* max_elems);
 /* Choose labels to slice: repeatedly fix the label that most reduces the
  * largest intermediate (ties: least flop increase) until the largest
  * intermediate is <= 2^log2_target elements or `max_sliced` labels are

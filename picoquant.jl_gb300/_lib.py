@@ -95,6 +95,7 @@ SIGNATURES = [
                                  C.c_int, C.c_uint64, i32p, f64p, i64p]),
     ("pq_plan_greedy_many", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_double,
                                       C.c_double, C.c_int, C.c_uint64, C.c_int, i32p, f64p, i64p]),
+    ("pq_plan_cost", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_int, i32p, f64p, f64p]),
     ("pq_plan_choose_slices", C.c_int, [C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, i32p, C.c_int, i32p,
                                         C.c_int, C.c_double, i32p, C.POINTER(C.c_int)]),
     ("pq_measure_pairs", C.c_int, [vp, C.c_int, i32p, i32p, i32p, i64p, C.c_int, f32p, f64p]),

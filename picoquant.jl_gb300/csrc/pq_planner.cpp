@@ -356,6 +356,69 @@ int pq_plan_greedy_many(int n_leaves, const int32_t* leaf_ranks, const int32_t* 
   return PQ_OK;
 }
 
+int pq_plan_cost(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
+                 const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
+                 const int32_t* out_labels, double* cmacs, double* max_elems) {
+  if (n_leaves < 1 || !leaf_ranks || n_steps < 0 || (n_steps && !steps) || (n_out && !out_labels) || !cmacs ||
+      !max_elems || n_labels < 0 || (n_labels && !label_dims))
+    return PQ_ERR_INVALID;
+  std::vector<double> l2dim(n_labels);
+  for (int i = 0; i < n_labels; ++i) {
+    if (label_dims[i] < 1) return PQ_ERR_INVALID;
+    l2dim[i] = std::log2((double)label_dims[i]);
+  }
+  std::vector<std::vector<int>> lab(n_leaves + n_steps);
+  std::vector<int> cnt(n_labels, 0);
+  int pos = 0;
+  for (int i = 0; i < n_leaves; ++i) {
+    if (leaf_ranks[i] < 0) return PQ_ERR_INVALID;
+    for (int j = 0; j < leaf_ranks[i]; ++j) {
+      const int x = leaf_labels[pos++];
+      if (x < 0 || x >= n_labels) return PQ_ERR_INVALID;
+      lab[i].push_back(x);
+      cnt[x]++;
+    }
+  }
+  for (int i = 0; i < n_out; ++i) {
+    if (out_labels[i] < 0 || out_labels[i] >= n_labels) return PQ_ERR_INVALID;
+    cnt[out_labels[i]]++;
+  }
+  std::vector<uint32_t> seen(n_labels, 0);
+  uint32_t stamp = 0;
+  double cost = 0, mx = 0;
+  std::vector<int> uni;
+  for (int s = 0; s < n_steps; ++s) {
+    const int x = steps[2 * s], y = steps[2 * s + 1];
+    if (x < 0 || y < 0 || x >= n_leaves + s || y >= n_leaves + s) return PQ_ERR_INVALID;
+    for (int l : lab[x]) cnt[l]--;
+    for (int l : lab[y]) cnt[l]--;
+    // the union of both label lists, first occurrences in order
+    ++stamp;
+    uni.clear();
+    for (const auto* side : {&lab[x], &lab[y]})
+      for (int l : *side)
+        if (seen[l] != stamp) {
+          seen[l] = stamp;
+          uni.push_back(l);
+        }
+    double l2u = 0, l2k = 0;
+    std::vector<int>& keep = lab[n_leaves + s];
+    for (int l : uni) {
+      l2u += l2dim[l];
+      if (cnt[l] > 0) keep.push_back(l);
+    }
+    for (int l : keep) {
+      cnt[l]++;
+      l2k += l2dim[l];
+    }
+    cost += std::exp2(l2u);
+    mx = std::max(mx, l2k);
+  }
+  *cmacs = cost;
+  *max_elems = std::exp2(mx);
+  return PQ_OK;
+}
+
 int pq_plan_choose_slices(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
                           const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
                           const int32_t* out_labels, int max_sliced, double log2_target, int32_t* sliced,

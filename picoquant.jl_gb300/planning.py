@@ -389,34 +389,17 @@ def bitstrings_to_index(bitstrings):
 def plan_cost(ranks, flat, dims, steps, out_labels):
     """Complex multiply-adds and largest intermediate (elements) of SSA steps,
     with the label rule of the executor (a label is summed once no other live
-    tensor and no output carries it)."""
-    labs = []
-    pos = 0
-    cnt: dict[int, int] = {}
-    for r in ranks:
-        l = flat[pos:pos + r]
-        pos += r
-        labs.append(l)
-        for x in l:
-            cnt[x] = cnt.get(x, 0) + 1
-    for x in out_labels:
-        cnt[x] = cnt.get(x, 0) + 1
-    l2 = [float(np.log2(d)) for d in dims]
-    cost, mx = 0.0, 0.0
-    for i in range(len(steps) // 2):
-        a, b = labs[steps[2 * i]], labs[steps[2 * i + 1]]
-        for x in a:
-            cnt[x] -= 1
-        for x in b:
-            cnt[x] -= 1
-        union = list(dict.fromkeys(a + b))
-        keep = [x for x in union if cnt[x] > 0]
-        for x in keep:
-            cnt[x] += 1
-        labs.append(keep)
-        cost += 2.0 ** sum(l2[x] for x in union)
-        mx = max(mx, sum(l2[x] for x in keep))
-    return cost, 2.0 ** mx
+    tensor and no output carries it); computed natively (``pq_plan_cost``)."""
+    lib = L.lib()
+    cm, mx = C.c_double(), C.c_double()
+    i32 = [np.ascontiguousarray(np.asarray(v, dtype=np.int64).reshape(-1), dtype=np.int32)
+           if len(v) else np.zeros(1, np.int32) for v in (ranks, flat, steps, out_labels)]
+    d64 = np.ascontiguousarray(np.asarray(dims, dtype=np.int64).reshape(-1)) if len(dims) else np.zeros(1, np.int64)
+    p32 = [a.ctypes.data_as(L.i32p) for a in i32]
+    rc = lib.pq_plan_cost(len(ranks), p32[0], p32[1], len(dims), d64.ctypes.data_as(L.i64p), len(steps) // 2, p32[2],
+                          len(out_labels), p32[3], C.byref(cm), C.byref(mx))
+    L.check(rc, None, "pq_plan_cost")
+    return cm.value, mx.value
 
 
 def _node_qubit(network, node_label):

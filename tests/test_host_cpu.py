@@ -283,3 +283,64 @@ def test_network_json_round_trip(pq, O, host_backend):
     pq.contract_network(net2, pq.random_contraction_plan(net2, np.random.default_rng(0)))
     amp = complex(np.asarray(pq.load_tensor_data(net2, "result")).reshape(-1)[0])
     assert abs(amp - 1 / np.sqrt(2)) < 1e-12
+
+
+def _cost_restated(ranks, flat, dims, steps, out_labels):
+    """The executor's label rule restated in Python: a label is summed once
+    no other live tensor and no output carries it."""
+    labs, pos, cnt = [], 0, {}
+    for r in ranks:
+        lab = list(flat[pos:pos + r])
+        pos += r
+        labs.append(lab)
+        for x in lab:
+            cnt[x] = cnt.get(x, 0) + 1
+    for x in out_labels:
+        cnt[x] = cnt.get(x, 0) + 1
+    l2 = [float(np.log2(d)) for d in dims]
+    cost, mx = 0.0, 0.0
+    for i in range(len(steps) // 2):
+        a, b = labs[steps[2 * i]], labs[steps[2 * i + 1]]
+        for x in a + b:
+            cnt[x] -= 1
+        union = list(dict.fromkeys(a + b))
+        keep = [x for x in union if cnt[x] > 0]
+        for x in keep:
+            cnt[x] += 1
+        labs.append(keep)
+        cost += 2.0 ** sum(l2[x] for x in union)
+        mx = max(mx, sum(l2[x] for x in keep))
+    return cost, 2.0 ** mx
+
+
+def test_native_plan_cost_matches_label_rule(pq, host_backend):
+    """pq_plan_cost against the restated rule: every candidate plan of a 3x4
+    depth-8 single amplitude (exact), and random networks with extents 1..6,
+    repeated and open labels (to 1e-12)."""
+    from pqgb300 import costmodel as CM
+    from pqgb300 import planning as PL
+
+    gates = pq.random_grid_gates(3, 4, 8, seed=2)
+    net = pq.build_network(12, gates, decompose=True, backend=host_backend)
+    pq.add_input(net, "0" * 12)
+    pq.add_output(net, "010011010110")
+    nodes, ranks, flat, dims, _ = CM._leaf_arrays(net, [])
+    cands, _ = CM.candidate_plans(net, [], 8, 0)
+    for c in cands:
+        assert PL.plan_cost(ranks, flat, dims, c["steps"], []) == _cost_restated(ranks, flat, dims, c["steps"], [])
+    rng = np.random.default_rng(0)
+    for _ in range(40):
+        nl, nlab = int(rng.integers(2, 12)), int(rng.integers(3, 14))
+        dims = [int(x) for x in rng.integers(1, 7, nlab)]
+        ranks = [int(x) for x in rng.integers(1, 4, nl)]
+        flat = [int(x) for x in rng.integers(0, nlab, sum(ranks))]
+        out = [int(x) for x in rng.choice(nlab, int(rng.integers(0, 3)), replace=False)]
+        live, steps, nxt = list(range(nl)), [], nl
+        while len(live) > 1:
+            i, j = rng.choice(len(live), 2, replace=False)
+            x, y = live[i], live[j]
+            steps += [x, y]
+            live = [v for v in live if v not in (x, y)] + [nxt]
+            nxt += 1
+        got, ref = PL.plan_cost(ranks, flat, dims, steps, out), _cost_restated(ranks, flat, dims, steps, out)
+        assert np.allclose(got, ref, rtol=1e-12, atol=0)
