@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // (a tile's rows and exponent are looked up once per tile).
     const int64_t ntl = blockIdx.x < ntot ? (ntot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const int64_t items = ntl * ktiles;
-    int64_t ptl = -1;  // tile (number within this CTA) of the row below
+    int64_t ptl = -1;  // tile (number within this CTA) whose row pointer and exponent are cached
     const TA* prow = A;
     bool pm = false;
     int en = kExpZero;  // exponent of the prefetched K tile's row (a load in flight)
