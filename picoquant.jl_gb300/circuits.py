@@ -137,7 +137,8 @@ def fuse_gates(gates, max_qubits=4):
     its qubits' latest blocks differ, those blocks are merged with it if each
     is still the latest on all of its own qubits (so it can move past every
     block in between, which acts on other qubits) and the union fits; else
-    the gate starts a block.  Exact: only commuting blocks are reordered."""
+    the gate starts a block (a gate wider than ``max_qubits`` is a block of
+    its own).  Exact: only commuting blocks are reordered."""
     blocks = []   # [qubits (first = low bit), matrix, alive]
     last = {}     # qubit -> index of its latest block
     for U, qs in gates:
