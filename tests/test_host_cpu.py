@@ -344,3 +344,23 @@ def test_native_plan_cost_matches_label_rule(pq, host_backend):
             nxt += 1
         got, ref = PL.plan_cost(ranks, flat, dims, steps, out), _cost_restated(ranks, flat, dims, steps, out)
         assert np.allclose(got, ref, rtol=1e-12, atol=0)
+
+
+def test_flop_planner_statevector_candidate_on_fused_circuit(pq, O, host_backend):
+    """The flop-count planner with the gate-by-gate state-vector order among
+    its candidates, on a circuit fused into blocks of up to four qubits: the
+    chosen plan, contracted on the host backend, gives the state vector of the
+    unfused circuit; the state-vector order itself is valid and exact too."""
+    from pqgb300 import circuits as CI
+
+    gates = pq.random_grid_gates(3, 4, 10, seed=5)
+    for cands in (("sweep", "greedy", "wavefunction", "statevector"), ("statevector",)):
+        be = type(host_backend)()
+        net = pq.build_network(12, CI.fuse_gates(gates, 4), backend=be)
+        pq.add_input(net, "0" * 12)
+        steps, cm, mx, name = pq.planning.best_flop_plan(net, trials=2, candidates=cands)
+        assert name in cands and cm > 0 and mx >= 2 ** 12
+        _ssa_valid(steps, len(net.nodes))
+        pq.contract_network(net, pq.steps_to_pairs(net, steps))
+        out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
+        assert np.max(np.abs(out - O.statevector(12, gates))) < 1e-12
