@@ -103,6 +103,12 @@ class ClockSampler:
 # workloads
 # ---------------------------------------------------------------------------
 
+# randomized qubit-sweep orders joining the sweep candidates of the 6x6
+# depth-16 plans (every arm: mixed precision, plain FP64, CPU sample), seeded;
+# planning is outside the timed region
+SWEEP_RANDOM = 64
+
+
 def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026, rank=0, target=28.0,
                  planner="learned"):
     n = rows * cols
@@ -117,11 +123,12 @@ def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026
 
     if planner == "learned" and CM.WEIGHTS_FILE.exists():
         model = CM.CostModel.load(be)
-        chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=4)
+        chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=4, n_sweep_random=SWEEP_RANDOM)
         model.close()
         steps, cm, mx, name = chosen["steps"], chosen["cmacs"], chosen["max_elems"], "learned:" + chosen["name"]
     else:
-        steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+        steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",),
+                                                         sweep_random=SWEEP_RANDOM)
     plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
     sliced = plan.choose_slices(max_sliced=n_sliced, log2_target=target)
     t_plan = time.perf_counter() - t0
@@ -574,7 +581,8 @@ def _cpu_sample_sliced(pq, O, args, rows=6, cols=6, depth=16):
     net = pq.build_network(n, gates, decompose=True, backend=host)
     pq.add_input(net, "0" * n)
     pq.add_output(net, bits)
-    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",),
+                                                     sweep_random=SWEEP_RANDOM)
     nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
     # find the heaviest step and its operand labels
     labs, pos = [], 0

@@ -239,9 +239,11 @@ def train_cost_model(backend, n_pairs=200_000, seed=0, epochs=40, reps=3, log=No
 # learned planner
 # ---------------------------------------------------------------------------
 
-def candidate_plans(network, out_edges=None, n_random=16, seed=0):
-    """Candidate SSA plans: the qubit sweep, the reference's full-wavefunction
-    order (for open outputs), plain greedy and Boltzmann-greedy draws."""
+def candidate_plans(network, out_edges=None, n_random=16, seed=0, n_sweep_random=0):
+    """Candidate SSA plans: the qubit sweeps (with ``n_sweep_random``
+    randomized sweep orders, the cheapest few kept), the reference's
+    full-wavefunction order (for open outputs), plain greedy and
+    Boltzmann-greedy draws."""
     if out_edges is None:
         out_edges = open_output_edges(network)
     nodes, ranks, flat, dims, label_of = _leaf_arrays(network, out_edges)
@@ -249,7 +251,8 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
     out = []
     # the sweep and native greedy planners return their own cost and largest
     # intermediate (the same label rule as plan_cost)
-    for i, (s, c, m) in enumerate(sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, all_orders=True)):
+    for i, (s, c, m) in enumerate(sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, all_orders=True,
+                                              random_orders=n_sweep_random, seed=seed)):
         out.append({"name": f"sweep{i}", "steps": s, "cmacs": c, "max_elems": m})
     if not out_edges or all(network.edges[e].src is not None for e in network.input_qubits):
         try:
@@ -265,7 +268,7 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0):
 
 
 def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_factor=8.0, max_elems=2**30,
-                 slice_targets=(), max_sliced=10, batch=1024, timings=None):
+                 slice_targets=(), max_sliced=10, batch=1024, timings=None, n_sweep_random=0):
     """Rank candidate plans -- and, with ``slice_targets``, candidate slicing
     sets of each (the slice chooser at each target, log2 elements, for plans
     whose largest intermediate exceeds the largest target) -- by the model's
@@ -277,7 +280,7 @@ def learned_plan(network, model, out_edges=None, n_random=16, seed=0, flop_facto
     slicing sets were ranked, its best ``sliced`` edge list.  ``timings``, a
     dict, receives the seconds spent generating and ranking candidates."""
     t0 = time.perf_counter()
-    cands, out_edges = candidate_plans(network, out_edges, n_random, seed)
+    cands, out_edges = candidate_plans(network, out_edges, n_random, seed, n_sweep_random)
     t1 = time.perf_counter()
     best_flop = min(cands, key=lambda c: (c["cmacs"], c["max_elems"]))
     for c in cands:

@@ -411,13 +411,17 @@ def _node_qubit(network, node_label):
 
 
 def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None, flat=None, dims=None,
-                all_orders=False):
+                all_orders=False, random_orders=0, keep_random=4, seed=0):
     """Qubit-sweep plan: contract each qubit's tensors along time into one
     tensor, then absorb qubits one at a time into a growing boundary.
 
     Several qubit orders are tried (natural and reversed order, and greedy
-    smallest-boundary orders started from a few qubits); the cheapest by
-    complex multiply-adds is returned as (steps, cmacs, max_elems), or every
+    smallest-boundary orders started from a few qubits); with
+    ``random_orders``, that many seeded randomized boundary-greedy orders too
+    (a random start, each next qubit drawn with weight 2^(-boundary / T) over
+    the frontier, T cycling through 0.3, 0.7, 1.5 in log2 elements), of which
+    the ``keep_random`` cheapest are kept.  The cheapest by complex
+    multiply-adds is returned as (steps, cmacs, max_elems), or every kept
     order's triple when ``all_orders``.
     """
     leaves = leaves if leaves is not None else list(network.nodes.keys())
@@ -470,7 +474,7 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
         for q in ow:
             adj[q].update(p for p in ow if p != q)
 
-    def greedy_order(start):
+    def greedy_order(start, rng=None, temp=1.0):
         # the boundary after absorbing a set of groups: the labels of absorbed
         # groups still held by an unabsorbed group or open; rem[x] counts the
         # unabsorbed groups holding x, so one candidate's boundary is the
@@ -510,10 +514,16 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
             if not cands:
                 cands = set(qs) - absorbed
             best, bl = None, None
-            for c in sorted(cands):
-                b = after(c)
-                if bl is None or b < bl - 1e-9:
-                    best, bl = c, b
+            if rng is None:
+                for c in sorted(cands):
+                    b = after(c)
+                    if bl is None or b < bl - 1e-9:
+                        best, bl = c, b
+            else:
+                cs = sorted(cands)
+                b = np.array([after(c) for c in cs])
+                w = np.exp2(-(b - b.min()) / temp)
+                best = cs[int(rng.choice(len(cs), p=w / w.sum()))]
             order.append(best)
             absorbed.add(best)
             absorb(best)
@@ -525,8 +535,7 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
     starts = [qs[0], qs[-1], qs[nq // 2], qs[nq // 4], qs[(3 * nq) // 4]]
     for s in dict.fromkeys(starts):
         orders.append(greedy_order(s))
-    found = []
-    for order in orders:
+    def order_steps(order):
         steps = list(base_steps)
         n2 = nxt
         v = group_val[order[0]]
@@ -534,17 +543,38 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
             steps += [v, group_val[q]]
             v = n2
             n2 += 1
-        c, m = plan_cost(ranks, flat, dims, steps, out_labels)
-        found.append((steps, c, m))
+        return steps
+
+    found = []
+    for order in orders:
+        steps = order_steps(order)
+        found.append((steps, *plan_cost(ranks, flat, dims, steps, out_labels)))
+    if random_orders > 0:
+        rng = np.random.default_rng(seed)
+        temps = (0.3, 0.7, 1.5)
+        seen = {tuple(o) for o in orders}
+        extra = []
+        for i in range(random_orders):
+            o = greedy_order(qs[int(rng.integers(nq))], rng, temps[i % len(temps)])
+            if tuple(o) in seen:
+                continue
+            seen.add(tuple(o))
+            steps = order_steps(o)
+            extra.append((steps, *plan_cost(ranks, flat, dims, steps, out_labels)))
+        extra.sort(key=lambda t: (t[1], t[2]))
+        found += extra[:keep_random]
     if all_orders:
         return found
     return min(found, key=lambda t: (t[1], t[2]))
 
 
-def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("sweep", "greedy", "wavefunction")):
+def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("sweep", "greedy", "wavefunction"),
+                   sweep_random=0):
     """The flop-count planner: the cheapest (complex multiply-adds) of the
     candidate plans ("sweep", "greedy", "wavefunction" and the gate-by-gate
-    "statevector" order).  Returns (steps, cmacs, max_elems, name)."""
+    "statevector" order); ``sweep_random`` randomized qubit-sweep orders join
+    the sweep candidates (``sweep_steps``).  Returns (steps, cmacs, max_elems,
+    name)."""
     if out_edges is None:
         out_edges = open_output_edges(network)
     nodes, ranks, flat, dims, label_of = _leaf_arrays(network, out_edges)
@@ -554,7 +584,8 @@ def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("swee
         s, c, m = greedy_steps(ranks, flat, dims, outl, 1.0, 1.0, trials, seed)
         found.append((s, *plan_cost(ranks, flat, dims, s, outl), "greedy"))
     if "sweep" in candidates:
-        s, c, m = sweep_steps(network, nodes, outl, label_of, ranks, flat, dims)
+        s, c, m = sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, random_orders=sweep_random,
+                              seed=seed)
         found.append((s, c, m, "sweep"))
     if "wavefunction" in candidates and all(network.edges[e].src is not None for e in network.input_qubits):
         try:

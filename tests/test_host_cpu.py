@@ -364,3 +364,32 @@ def test_flop_planner_statevector_candidate_on_fused_circuit(pq, O, host_backend
         pq.contract_network(net, pq.steps_to_pairs(net, steps))
         out = pq.load_tensor_data(net, "result").reshape(-1, order="F")
         assert np.max(np.abs(out - O.statevector(12, gates))) < 1e-12
+
+
+def test_randomized_sweep_orders(pq, O, host_backend):
+    """Seeded randomized qubit-sweep orders: valid SSA plans, reproducible for
+    a seed, never costlier than the deterministic sweeps (the cheapest is
+    kept), and the chosen plan contracted on the host backend gives the
+    state vector's amplitude."""
+    from pqgb300 import costmodel as CM
+    from pqgb300 import planning as PL
+
+    n, bits = 12, "011010011100"
+    gates = pq.random_grid_gates(3, 4, 10, seed=7)
+    net = pq.build_network(n, gates, decompose=True, backend=host_backend)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    nodes, ranks, flat, dims, label_of = CM._leaf_arrays(net, [])
+    det = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims)
+    rnd = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, random_orders=32, seed=3)
+    again = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, random_orders=32, seed=3)
+    assert rnd[0] == again[0] and rnd[1] <= det[1]
+    allo = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, all_orders=True, random_orders=32, seed=3,
+                          keep_random=4)
+    assert 7 <= len(allo) <= 7 + 4 and min(c for _, c, _ in allo) == rnd[1]
+    for steps, cm, mx in allo:
+        _ssa_valid(steps, len(nodes))
+        assert PL.plan_cost(ranks, flat, dims, steps, []) == (cm, mx)
+    pq.contract_network(net, pq.steps_to_pairs(net, rnd[0]))
+    amp = complex(np.asarray(pq.load_tensor_data(net, "result")).reshape(-1)[0])
+    assert abs(amp - O.statevector(n, gates)[O.amplitude_index(bits)]) < 1e-12
