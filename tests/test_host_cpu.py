@@ -393,3 +393,30 @@ def test_randomized_sweep_orders(pq, O, host_backend):
     pq.contract_network(net, pq.steps_to_pairs(net, rnd[0]))
     amp = complex(np.asarray(pq.load_tensor_data(net, "result")).reshape(-1)[0])
     assert abs(amp - O.statevector(n, gates)[O.amplitude_index(bits)]) < 1e-12
+
+
+def test_bench_roofline_classes():
+    """The bench's roofline assembly over per-step timings: every kernel class
+    (generic, SIMT GEMM, tcgen05, copy, skinny) is named, shares add up, and
+    the dominant class decides the bound (HBM for the skinny class, tensor
+    for tcgen05, with the exact scheme's tensor work per algorithmic flop)."""
+    import bench
+
+    peaks = {"hbm_gbs": 6757.5, "bf16_tflops": 1871.0, "bf16_tflops_sustained": 1683.9}
+
+    def feats(kc, lc, lk, nbytes):
+        return [10.0, 10.0, lc, lk, 1.0, 1.0, float(kc), nbytes]
+
+    steps = [(0.2, False, feats(0, 10, 2, 1e6)), (3.0, False, feats(4, 28, 4, 4e9)),
+             (0.1, True, feats(3, 12, 0, 1e5)), (0.5, False, feats(1, 20, 8, 1e8))]
+    ms, batched, fs = zip(*steps)
+    roof, info = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki")
+    assert set(info) == {"generic", "skinny", "copy", "gemm_simt"}
+    assert abs(sum(d["share"] for d in info.values()) - 1.0) < 1e-12
+    assert roof["bound"] == "hbm" and roof["kernel"] == "skinny" and roof["unit"] == "GB/s"
+    assert abs(roof["achieved"] - 4e9 / 3e-3 / 1e9) < 1e-6 and roof["frac"] == roof["achieved"] / 6757.5
+    steps.append((9.0, False, feats(2, 28, 8, 5e9)))
+    ms, batched, fs = zip(*steps)
+    roof, info = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki")
+    assert roof["bound"] == "tensor" and roof["tensor_ops_per_algorithmic_flop"] == 15.0
+    assert abs(roof["achieved"] - 8.0 * 2 ** 28 * 2 ** 8 / 9e-3 / 1e12) < 1e-9
