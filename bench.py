@@ -110,7 +110,10 @@ SWEEP_RANDOM = 64
 
 
 def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026, rank=0, target=28.0,
-                 planner="learned"):
+                 planner="learned", steps=None):
+    """The sliced single-amplitude workload on a new backend of ``precision``:
+    network, plan (``steps`` if given, else the named planner's choice) and
+    the sliced bonds chosen for a 2^target-element intermediate limit."""
     n = rows * cols
     gates = pq.random_grid_gates(rows, cols, depth, seed=seed)
     bits = pq.random_bitstrings(n, 1, seed=seed + 1 + rank)[0]
@@ -121,7 +124,11 @@ def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026
     t0 = time.perf_counter()
     from pqgb300 import costmodel as CM
 
-    if planner == "learned" and CM.WEIGHTS_FILE.exists():
+    if steps is not None:
+        nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
+        cm, mx = pq.planning.plan_cost(ranks, flat, dims, steps, [])
+        name = "given"
+    elif planner == "learned" and CM.WEIGHTS_FILE.exists():
         model = CM.CostModel.load(be)
         chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=[], n_random=4, n_sweep_random=SWEEP_RANDOM)
         model.close()
@@ -133,7 +140,63 @@ def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026
     sliced = plan.choose_slices(max_sliced=n_sliced, log2_target=target)
     t_plan = time.perf_counter() - t0
     return dict(be=be, net=net, plan=plan, sliced=sliced, gates=gates, bits=bits, cmacs=cm, max_elems=mx,
-                planner=name, t_plan=t_plan, n=n)
+                planner=name, t_plan=t_plan, n=n, rows=rows, cols=cols, depth=depth, seed=seed,
+                bits_seed=seed + 1 + rank)
+
+
+# The 6x6 depth-16 plan the GB300 arm contracts, recorded for the CPU
+# reference arm (which must not load the product library to plan): written
+# by `python bench.py --write-plan oracle/plans/grid6x6_d16_sliced.json`.
+PLAN_FILE = ROOT / "oracle" / "plans" / "grid6x6_d16_sliced.json"
+
+
+def plan_record(w):
+    """The sliced workload's plan in a library-independent form: the
+    circuit's generator seeds, the leaves (node names and their index names
+    in node order), the SSA steps over them and the sliced bonds."""
+    net, plan = w["net"], w["plan"]
+    return {"workload": f"grid{w['rows']}x{w['cols']}_depth{w['depth']}_sliced_single_amplitude",
+            "rows": w["rows"], "cols": w["cols"], "depth": w["depth"], "circuit_seed": w["seed"],
+            "bitstring_seed": w["bits_seed"], "bitstring": w["bits"], "planner": w["planner"],
+            "log2_cmacs": float(np.log2(w["cmacs"])), "log2_max_elems": float(np.log2(w["max_elems"])),
+            "leaves": list(plan.leaves), "leaf_indices": [list(net.nodes[x].indices) for x in plan.leaves],
+            "steps": [int(x) for x in plan.steps], "sliced": list(w["sliced"])}
+
+
+def oracle_network(O, rec):
+    """The record's network built by the oracle's own circuit generator and
+    graph code; its leaves must be the record's (same node and index names in
+    the same order), so the record's SSA steps apply to it."""
+    rows, cols = rec["rows"], rec["cols"]
+    n = rows * cols
+    gates = O.random_grid_gates(rows, cols, rec["depth"], seed=rec["circuit_seed"])
+    net = O.build_network(n, gates, decompose=True, backend=O.OracleBackend())
+    O.add_input(net, "0" * n)
+    O.add_output(net, rec["bitstring"])
+    names = list(net.nodes.keys())
+    if names != rec["leaves"] or [list(net.nodes[x].indices) for x in names] != rec["leaf_indices"]:
+        raise RuntimeError("the oracle's network does not have the plan's leaves")
+    return net
+
+
+def oracle_amplitude(O, rec):
+    """The record's amplitude contracted by the FP64 oracle (numpy tensordot
+    -> BLAS zgemm) along the record's steps, unsliced; returns (amplitude,
+    seconds of the contraction itself)."""
+    net = oracle_network(O, rec)
+    t0 = time.perf_counter()
+    r = O.contract_along_steps(net, rec["steps"])
+    dt = time.perf_counter() - t0
+    return complex(np.asarray(r).reshape(-1)[0]), dt
+
+
+def host_threads():
+    """BLAS threads of the host arm: OPENBLAS_NUM_THREADS / OMP_NUM_THREADS
+    when set, else every core (OpenBLAS's default)."""
+    for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS"):
+        if os.environ.get(v, "").isdigit():
+            return int(os.environ[v])
+    return os.cpu_count()
 
 
 def leaf_host_data(pq, w, dtype):
@@ -171,11 +234,16 @@ def main():
     ap.add_argument("--depth", type=int, default=16)
     ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "6xtf32", "ozaki", "3xbf16", "c128"])
     ap.add_argument("--batch", type=int, default=0, help="slices per launch (0: sized from memory)")
-    ap.add_argument("--cpu-log2", type=float, default=31.0, help="log2 complex MACs of the CPU sample")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="seconds of whole-amplitude CPU steps the reference arm times (at least one step)")
+    ap.add_argument("--oracle", default="full", choices=["full", "skip"],
+                    help="contract the headline amplitude with the FP64 oracle too (rel_err_vs_oracle, cpu_baseline)")
+    ap.add_argument("--write-plan", default="", help="write the sliced workload's plan record to this JSON file")
     ap.add_argument("--slice-target", type=float, default=28.0,
                     help="log2 elements allowed per slice intermediate when choosing sliced bonds")
     ap.add_argument("--fp64", default="full", choices=["full", "skip"],
-                    help="also run the plain complex-FP64 GPU path on the same amplitude")
+                    help="also run the plain complex-FP64 GPU path on the same amplitude and plan")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed runs of the plain complex-FP64 path")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -537,121 +605,73 @@ def run_pair(args):
 
 
 def run_reference(args):
+    """The CPU reference arm: the FP64 oracle (numpy restatement of the
+    reference's contraction semantics, tensordot -> BLAS zgemm on every host
+    core) timed on the same workload.  It imports neither the product
+    package nor its library: the 6x6 depth-16 amplitude is contracted along
+    the plan recorded in ``PLAN_FILE`` (the GB300 arm's plan), the network
+    built by the oracle's own generator.  A step is one whole amplitude
+    (about a minute on 16 cores), so the arm times as many steps as fit
+    ``--ref-budget`` seconds (at least one, at most ``--steps``); CPU runs
+    need no warm-up."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import tn_oracle as O  # the FP64 CPU restatement (reference arm)
 
-    import __graft_entry__ as g
-
-    pq = g.load_package()
-    cores = os.cpu_count()
-    rows, cols, depth = (args.rows, args.cols, args.depth) if args.workload == "grid6x6_d16_sliced" else (4, 5, 12)
-    val, sample = cpu_sample(pq, O, args, rows, cols, depth)
-    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "amplitudes/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+    cores = host_threads()
+    base = {"impl": "reference", "metric": METRIC, "unit": "amplitudes/s", "n_gpus": args.gpus,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic"}
+    if args.workload == "grid6x6_d16_sliced":
+        rows, cols, depth = args.rows, args.cols, args.depth
+        if not PLAN_FILE.exists() or (rows, cols, depth) != (6, 6, 16):
+            print(json.dumps({"impl": "reference", "unavailable": f"no recorded plan for grid{rows}x{cols} depth "
+                                                                  f"{depth} ({PLAN_FILE.name} covers 6x6 depth 16)"}))
+            return 0
+        rec = json.loads(PLAN_FILE.read_text())
+        times, amp = [], None
+        t_start = time.perf_counter()
+        while len(times) < max(1, args.steps):
+            amp, dt = oracle_amplitude(O, rec)
+            times.append(dt)
+            if time.perf_counter() - t_start + dt > args.ref_budget:
+                break
+        val = len(times) / sum(times)
+        sample = (f"timed: {len(times)} whole amplitude(s) of the 6x6 depth-16 circuit, each contracted unsliced "
+                  f"by the FP64 oracle (numpy tensordot -> BLAS zgemm, {cores} threads) along the GB300 arm's plan "
+                  f"({rec['planner']}, 2^{rec['log2_cmacs']:.2f} complex MACs, read from {PLAN_FILE.name}); "
+                  f"{np.mean(times):.1f} s per amplitude")
+        extra = {"amplitude": [amp.real, amp.imag], "steps_requested": args.steps,
+                 "plan_sha": plan_sha(rec["steps"])}
+    else:
+        rows, cols, depth = 4, 5, 12
+        val, sample = _cpu_sample_amps(O, rows, cols, depth)
+        times, extra = [1024 / val], {}
+    line = {**base, "value": val, "steps": len(times), "warmup": 0, "ms_per_step": 1e3 * float(np.mean(times)),
             "config": workload_config(args, rows, cols, depth),
             "cpu_baseline": {"value": val, "unit": "amplitudes/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "amplitudes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line))
     return 0
+
+
+def plan_sha(steps):
+    import hashlib
+
+    return hashlib.sha256(",".join(str(int(x)) for x in steps).encode()).hexdigest()[:16]
 
 
 def workload_config(args, rows, cols, depth):
     if args.workload == "grid6x6_d16_sliced":
         return {"workload": f"grid{rows}x{cols}_depth{depth}_sliced_single_amplitude", "qubits": rows * cols,
                 "depth": depth, "sliced_bonds": 10, "slices": 1024, "batch": args.batch,
-                "plan": "learned cost model over qubit-sweep orders (flop-count planner judges; plain FP64 "
-                        "path uses the flop-count plan)", "l2": "flushed between steps (256 MiB write)"}
+                "plan": "learned cost model over qubit-sweep orders (flop-count planner judges); the plain FP64 "
+                        "GPU path, the FP64 oracle and the CPU reference arm contract the same plan",
+                "l2": "flushed between steps (256 MiB write)"}
     return {"workload": f"grid{rows}x{cols}_depth{depth}_1024_amplitudes", "qubits": rows * cols, "depth": depth,
             "amplitudes_per_step": 1024,
             "plan": "flop-count planner over the circuit fused into blocks of up to four qubits (open outputs + "
                     "gather)",
             "l2": "flushed between steps (256 MiB write)"}
-
-
-def _cpu_sample_sliced(pq, O, args, rows=6, cols=6, depth=16):
-    """CPU FP64 rate on the plan's heaviest pairwise step, shrunk to about
-    2^(args.cpu_log2) complex multiply-adds by fixing free modes of the larger
-    operand; the amplitude time is the plan's total complex multiply-adds over
-    that measured rate."""
-    host = _HostStore()
-    n = rows * cols
-    gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
-    bits = pq.random_bitstrings(n, 1, seed=2027)[0]
-    net = pq.build_network(n, gates, decompose=True, backend=host)
-    pq.add_input(net, "0" * n)
-    pq.add_output(net, bits)
-    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",),
-                                                     sweep_random=SWEEP_RANDOM)
-    nodes, ranks, flat, dims, label_of = pq.planning._leaf_arrays(net, [])
-    # find the heaviest step and its operand labels
-    labs, pos = [], 0
-    for r in ranks:
-        labs.append(list(flat[pos:pos + r]))
-        pos += r
-    cnt = {}
-    for l in labs:
-        for x in l:
-            cnt[x] = cnt.get(x, 0) + 1
-    best = None
-    for i in range(len(steps) // 2):
-        la, lb = labs[steps[2 * i]], labs[steps[2 * i + 1]]
-        for x in la + lb:
-            cnt[x] -= 1
-        union = list(dict.fromkeys(la + lb))
-        keep = [x for x in union if cnt[x] > 0]
-        for x in keep:
-            cnt[x] += 1
-        labs.append(keep)
-        c = float(np.prod([dims[x] for x in union], dtype=np.float64))
-        if best is None or c > best[0]:
-            best = (c, la, lb)
-    c, la, lb = best
-    common = [x for x in la if x in lb]
-    # shrink: fix free modes of the larger operand until ~2^cpu_log2 MACs
-    big, small = (la, lb) if np.prod([dims[x] for x in la]) >= np.prod([dims[x] for x in lb]) else (lb, la)
-    fixed = set()
-    work = c
-    for x in big:
-        if work <= 2.0 ** args.cpu_log2:
-            break
-        if x not in common:
-            fixed.add(x)
-            work /= dims[x]
-    rng = np.random.default_rng(0)
-    shp_b = [1 if x in fixed else dims[x] for x in big]
-    shp_s = [dims[x] for x in small]
-    A = rng.standard_normal(shp_b) + 1j * rng.standard_normal(shp_b)
-    B = rng.standard_normal(shp_s) + 1j * rng.standard_normal(shp_s)
-    axes = ([big.index(x) for x in common], [small.index(x) for x in common])
-    np.tensordot(A, B, axes=axes)  # warm
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
-        np.tensordot(A, B, axes=axes)
-        reps += 1
-        if time.perf_counter() - t0 > 2.0:
-            break
-    dt = (time.perf_counter() - t0) / reps
-    rate = work / dt  # complex MACs / s
-    desc = (f"heaviest step of the plan ({np.log2(c):.1f} log2 complex MACs) shrunk to 2^{np.log2(work):.1f} "
-            f"by fixing free modes, numpy tensordot FP64 (BLAS zgemm, {os.cpu_count()} threads) at "
-            f"{rate * 8 / 1e9:.1f} GFLOP/s; amplitude time = plan total 2^{np.log2(cm):.2f} complex MACs / rate")
-    return rate / cm, desc
-
-
-def _choose(pq, ranks, flat, dims, steps, k):
-    import ctypes as C
-
-    from pqgb300 import _lib as L
-
-    out = (C.c_int32 * k)()
-    ns = C.c_int()
-    rc = L.lib().pq_plan_choose_slices(len(ranks), L.arr(C.c_int32, ranks), L.arr(C.c_int32, flat), len(dims),
-                                       L.arr(C.c_int64, dims), len(steps) // 2, L.arr(C.c_int32, steps), 0,
-                                       L.arr(C.c_int32, []), k, 0.0, out, C.byref(ns))
-    L.check(rc, None, "choose_slices")
-    return [out[i] for i in range(ns.value)]
 
 
 class _HostStore:
@@ -670,22 +690,17 @@ class _HostStore:
         return self.tensors[label].shape
 
 
-def _cpu_sample_amps(pq, O, n_amps, rows=4, cols=5, depth=12):
+def _cpu_sample_amps(O, rows=4, cols=5, depth=12):
+    """1024 amplitudes of the 4x5 depth-12 circuit from the oracle's FP64
+    state vector (one tensordot per gate), timed."""
     n = rows * cols
-    gates = pq.random_grid_gates(rows, cols, depth, seed=2024)
+    gates = O.random_grid_gates(rows, cols, depth, seed=2024)
     t0 = time.perf_counter()
     sv = O.statevector(n, gates)
-    bits = pq.random_bitstrings(n, 1024, seed=7)
+    bits = O.random_bitstrings(n, 1024, seed=7)
     _ = sv[[O.amplitude_index(b) for b in bits]]
     dt = time.perf_counter() - t0
-    return 1024 / dt, "full 1024 amplitudes via FP64 numpy state vector (tensordot per gate)"
-
-
-def cpu_sample(pq, O, args, rows, cols, depth):
-    """Time the FP64 CPU restatement on a bounded sample; returns (amplitudes/s, description)."""
-    if args.workload == "grid6x6_d16_sliced":
-        return _cpu_sample_sliced(pq, O, args, rows, cols, depth)
-    return _cpu_sample_amps(pq, O, 1024, rows, cols, depth)
+    return 1024 / dt, "timed: all 1024 amplitudes via the oracle's FP64 numpy state vector (tensordot per gate)"
 
 
 def run_gb300(args, world, rank):
@@ -822,54 +837,97 @@ def run_gb300(args, world, rank):
 
 def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, launches, clk, e2e, peaks, peaks_kind,
            prec_name, precision, result, world):
+    import torch
+
     sys.path.insert(0, str(ROOT / "oracle"))
-    import tn_oracle as O  # the FP64 CPU restatement, for the cpu_baseline leg only
+    import tn_oracle as O  # the FP64 oracle: the checker and the timed cpu_baseline leg only
+
+    import ctypes as C
 
     extra = {}
     roof = None
+    cpu = None
+    ms_step = 1e3 * t_total / args.steps
     if args.workload == "grid6x6_d16_sliced":
         sliced = w["sliced"]
         ms, batched, feats = plan.profile_sliced(sliced, batch=args.batch)
-        roof, kinfo = roofline_from_profile(ms, batched, feats, peaks, peaks_kind, 2 ** len(sliced) // args.batch,
-                                            prec_name)
+        roof, kinfo, overall = roofline_from_profile(ms, batched, feats, peaks, peaks_kind,
+                                                     2 ** len(sliced) // args.batch, prec_name, ms_step)
         extra["kernel_classes"] = kinfo
-        # the plain complex-FP64 CUDA path on the same amplitude, and the error
-        # of this precision against it
-        if args.fp64 == "full":
-            w64 = build_sliced(pq, pq.PREC_C128, rows, cols, depth, target=args.slice_target, planner="flop")
-            b64 = w64["plan"].auto_batch(w64["sliced"])
-            t0 = time.perf_counter()
-            a64 = w64["plan"].run_sliced(w64["sliced"], batch=b64)
-            t64 = time.perf_counter() - t0
-            extra["plain_fp64_gpu"] = {"value": 1.0 / t64, "unit": "amplitudes/s",
-                                       "sample": "the same amplitude, all slices, complex128 FP64 kernels"}
-            extra["speedup_vs_plain_fp64"] = value / extra["plain_fp64_gpu"]["value"]
-            extra["rel_err_vs_fp64"] = abs(result - a64) / abs(a64)
-            # the same error relative to the amplitude scale 2^(-n/2) (amplitudes
-            # of random circuits are Porter-Thomas distributed around it)
-            extra["err_vs_fp64_over_2^-n/2"] = abs(result - a64) / 2.0 ** (-rows * cols / 2)
-            w64["plan"].close()
-            w64["be"].close()
+        extra["roofline_all_steps"] = overall
+        rec = plan_record(w)
+        ref_rec = json.loads(PLAN_FILE.read_text()) if PLAN_FILE.exists() else None
+        if args.write_plan:
+            Path(args.write_plan).parent.mkdir(parents=True, exist_ok=True)
+            Path(args.write_plan).write_text(json.dumps(rec))
         extra["amplitude"] = [float(np.real(result)), float(np.imag(result))]
         extra["plan"] = {"planner": w["planner"], "cmacs_unsliced": w["cmacs"], "max_elems_unsliced": w["max_elems"],
-                         "sliced_bonds": len(sliced), "planning_s": w["t_plan"]}
+                         "sliced_bonds": len(sliced), "planning_s": w["t_plan"], "plan_sha": plan_sha(rec["steps"]),
+                         "same_plan_as_reference_arm": bool(ref_rec is not None and ref_rec["steps"] == rec["steps"]
+                                                            and ref_rec["leaves"] == rec["leaves"])}
+        # the plain complex-FP64 CUDA path on the same amplitude along the same
+        # plan, timed warm with CUDA events on its context's stream
+        a64 = None
+        if args.fp64 == "full":
+            w64 = build_sliced(pq, pq.PREC_C128, rows, cols, depth, target=args.slice_target, steps=plan.steps)
+            p64, s64 = w64["plan"], w64["sliced"]
+            b64 = p64.auto_batch(s64)
+            sp = C.c_void_p()
+            w64["be"].lib.pq_ctx_stream(w64["be"].ctx, C.byref(sp))
+            ext64 = torch.cuda.ExternalStream(sp.value)
+            for _ in range(2):  # warm-up; the second identical call records the CUDA graph
+                a64 = p64.run_sliced(s64, batch=b64)
+            ts64 = []
+            for _ in range(max(3, args.fp64_steps)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ext64)
+                a64 = p64.run_sliced(s64, batch=b64)
+                e1.record(ext64)
+                e1.synchronize()
+                ts64.append(e0.elapsed_time(e1))
+            extra["plain_fp64_gpu"] = {
+                "value": len(ts64) / (sum(ts64) / 1e3), "unit": "amplitudes/s", "steps": len(ts64),
+                "sliced_bonds": len(s64), "batch": b64,
+                "sample": "the same amplitude along the same plan, all slices, complex128 storage and FP64 kernels; "
+                          "2 warm-up runs, then CUDA events on the context's stream"}
+            extra["speedup_vs_plain_fp64"] = value / extra["plain_fp64_gpu"]["value"]
+            extra["rel_err_vs_fp64"] = abs(result - a64) / abs(a64)
+            p64.close()
+            w64["be"].close()
+        # the FP64 oracle's contraction of the same amplitude along the same
+        # plan (its own network build, numpy on the host): the parity check,
+        # and the timed CPU baseline
+        if args.oracle == "full":
+            amp_o, t_o = oracle_amplitude(O, rec)
+            extra["oracle"] = {"amplitude": [amp_o.real, amp_o.imag], "seconds": t_o, "threads": host_threads()}
+            extra["rel_err_vs_oracle"] = abs(result - amp_o) / abs(amp_o)
+            # relative to the amplitude scale 2^(-n/2) (amplitudes of random
+            # circuits are Porter-Thomas distributed around it)
+            extra["err_vs_oracle_over_2^-n/2"] = abs(result - amp_o) / 2.0 ** (-rows * cols / 2)
+            if a64 is not None:
+                extra["plain_fp64_gpu"]["rel_err_vs_oracle"] = abs(a64 - amp_o) / abs(amp_o)
+            cpu = {"value": 1.0 / t_o, "unit": "amplitudes/s", "cores": host_threads(), "kind": "port",
+                   "sample": f"timed: the whole amplitude contracted unsliced by the FP64 oracle (numpy tensordot -> "
+                             f"BLAS zgemm, {host_threads()} threads) along the same plan, once ({t_o:.1f} s)"}
     else:
         extra["plan"] = {"planner": w["planner"], "cmacs": w["cmacs"], "max_elems": w["max_elems"]}
         ms = w["plan"].profile()
         feats = w["plan"].features()
-        roof, kinfo = roofline_from_profile(ms, np.zeros(len(ms), bool), feats, peaks, peaks_kind, 1, prec_name)
+        roof, kinfo, overall = roofline_from_profile(ms, np.zeros(len(ms), bool), feats, peaks, peaks_kind, 1,
+                                                     prec_name, ms_step)
         extra["kernel_classes"] = kinfo
-    cpu_val, cpu_sample_desc = cpu_sample(__import__("__graft_entry__").load_package(), O, args, rows, cols, depth)
+        extra["roofline_all_steps"] = overall
+        v, desc = _cpu_sample_amps(O, rows, cols, depth)
+        cpu = {"value": v, "unit": "amplitudes/s", "cores": host_threads(), "kind": "port", "sample": desc}
     line = {
         "metric": METRIC, "value": value, "unit": "amplitudes/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"c64": "c64", "3xtf32": "c64(3xtf32)", "6xtf32": "c64(6xtf32)",
                                                            "ozaki": "c64(ozaki-bf16)", "3xbf16": "c64(3xbf16)",
                                                            "c128": "c128"}[prec_name],
         "data": "synthetic (seeded random circuits)", "config": workload_config(args, rows, cols, depth),
         "precision": prec_name, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-        "cpu_baseline": {"value": cpu_val, "unit": "amplitudes/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": cpu_sample_desc},
+        "cpu_baseline": cpu,
     }
     line.update(extra)
     return line
@@ -879,56 +937,91 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
 # 3xTF32 issues 3 split products of each of 4 real products, 6xTF32 6; the
 # exact-accumulation scheme 15 slice pairs of 4 real products.
 TENSOR_OPS_PER_FLOP = {"3xtf32": 3.0, "6xtf32": 6.0, "ozaki": 15.0}
-# DRAM bytes of the exact-accumulation GEMM kernel over its algorithmic bytes
-# (|A| + |B| + |C| once), from an ncu capture of the dominant pair at a
-# quarter height (M = 2^18, N = K = 256): 1.032 GB against 1.025 GB.
-OZ_GEMM_TRAFFIC_RATIO = 1.032 / 1.025
+# DRAM bytes of one exact-accumulation contraction step (row-exponent pass +
+# GEMM) over its algorithmic bytes (|A| + |B| + |C| once), from an ncu
+# capture of the dominant pair at a quarter height (M = 2^18, N = K = 256):
+# the GEMM moves 1.032 GB against 1.025 GB algorithmic, and the exponent pass
+# reads A (0.537 GB) once more.
+OZ_CLASS_TRAFFIC_RATIO = (1.032 + 0.537) / 1.025
+OZ_CLASS_TRAFFIC_SOURCE = ("k_oz_exp + k_oz_gemm DRAM bytes of the dominant pair at M = 2^18 (ncu), as a ratio "
+                           "to algorithmic bytes, scaled to this class's average algorithmic bytes per launch")
 
 
-def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks, prec_name=None):
-    """Dominant kernel class by device time; achieved algorithmic FLOP/s or
-    bytes/s of that class over its measured launch time."""
+# Nominal SIMT compute ceilings of a GB300 (not measured): FP32 = 152 SMs x
+# 128 lanes x 2 flop x 2.07 GHz; FP64 at GB300's reduced rate.  Only the
+# compute side of the SIMT kernel classes uses them; those classes are
+# memory-bound at the circuit shapes here (K <= 16 per gate).
+SIMT_TFLOPS = {"fp32": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 1.25}
+
+
+def roofline_from_profile(ms, batched, feats, peaks, peaks_kind, nchunks, prec_name=None, wall_ms=None):
+    """Per-step lower bounds t_p = max(B_p / BW, F_p / P) (B_p = algorithmic
+    bytes, each operand read once and the result written once at its storage
+    size; F_p = 8 |C| K real flops; P = the measured bf16 peak for the
+    tensor-core class, the nominal SIMT rate otherwise) against the measured
+    per-step device times.  Returns (roofline of the dominant kernel class by
+    device time, per-class summary, all-step summary).  The dominant class's
+    ``bound`` is the side with the larger summed lower bound; ``achieved`` is
+    its algorithmic bytes (or flops) over its measured time."""
     names = {0: "generic", 1: "gemm_simt", 2: "tcgen05", 3: "copy", 4: "skinny"}
+    bw = peaks.get("hbm_gbs") * 1e9
+    p_tc = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")) * 1e12
+    p_simt = SIMT_TFLOPS["fp64" if prec_name == "c128" else "fp32"] * 1e12
     info = {}
     for t, b, f in zip(ms, batched, feats):
         k = int(f[6])
         d = info.setdefault(names.get(k, str(k)), {"ms_per_run": 0.0, "launches_per_run": 0, "flops": 0.0,
-                                                    "bytes": 0.0, "ms_profiled": 0.0})
+                                                    "bytes": 0.0, "hbm_bound_ms": 0.0, "compute_bound_ms": 0.0,
+                                                    "lower_bound_ms": 0.0})
         rep = nchunks if b else 1
+        F = 8.0 * 2 ** f[2] * 2 ** f[3] * rep
+        B = f[7] * rep
+        th, tcmp = 1e3 * B / bw, 1e3 * F / (p_tc if k == 2 else p_simt)
         d["ms_per_run"] += t * rep
         d["launches_per_run"] += rep
-        d["flops"] += 8.0 * 2 ** f[2] * 2 ** f[3] * rep
-        d["bytes"] += f[7] * rep
+        d["flops"] += F
+        d["bytes"] += B
+        d["hbm_bound_ms"] += th
+        d["compute_bound_ms"] += tcmp
+        d["lower_bound_ms"] += max(th, tcmp)
     tot = sum(d["ms_per_run"] for d in info.values()) or 1.0
     for d in info.values():
         d["share"] = d["ms_per_run"] / tot
+        d["lower_bound_frac"] = d["lower_bound_ms"] / d["ms_per_run"] if d["ms_per_run"] else None
+    lb = sum(d["lower_bound_ms"] for d in info.values())
+    overall = {"lower_bound_ms": lb, "device_ms": tot, "wall_ms": wall_ms,
+               "frac_of_wall": lb / wall_ms if wall_ms else None,
+               "rule": "sum over steps of max(B_p / measured HBM copy, F_p / P) over the measured time"}
     dom = max(info, key=lambda k: info[k]["ms_per_run"])
     d = info[dom]
     secs = d["ms_per_run"] / 1e3
-    if dom in ("gemm_simt", "tcgen05"):
-        ach = d["flops"] / secs / 1e12
-        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": None, "kernel": dom, "peak_source": f"{peaks_kind} bf16 sustained",
-                "per_launch_ms": d["ms_per_run"] / d["launches_per_run"]}
-        if dom == "tcgen05" and prec_name in TENSOR_OPS_PER_FLOP:
-            r = TENSOR_OPS_PER_FLOP[prec_name]
-            roof.update({"kernel": "tcgen05 contraction steps (GEMM plus its scale / slice pre-passes)",
-                         "tensor_ops_per_algorithmic_flop": r, "tensor_work_tflops": ach * r,
-                         "tensor_work_frac": ach * r / peak})
-            if prec_name == "ozaki":
-                roof["traffic"] = d["bytes"] / d["launches_per_run"] * OZ_GEMM_TRAFFIC_RATIO
-                roof["traffic_unit"] = "bytes per launch"
-                roof["traffic_source"] = ("k_oz_gemm DRAM bytes per launch: ncu capture of the dominant pair at "
-                                          "M=2^18 (1.007 x algorithmic bytes), scaled to this class's average "
-                                          "algorithmic bytes per launch; the exponent pre-pass reads A once more")
-    else:
+    common = {"kernel": dom, "per_launch_ms": d["ms_per_run"] / d["launches_per_run"],
+              "launches_per_run": d["launches_per_run"], "lower_bound_frac": d["lower_bound_frac"]}
+    if d["hbm_bound_ms"] >= d["compute_bound_ms"]:
         ach = d["bytes"] / secs / 1e9
-        peak = peaks.get("hbm_gbs")
-        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
-                "kernel": dom, "peak_source": f"{peaks_kind} hbm copy",
-                "per_launch_ms": d["ms_per_run"] / d["launches_per_run"]}
-    return roof, info
+        roof = {"bound": "hbm", "achieved": ach, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": ach / peaks.get("hbm_gbs"), "traffic": None, "peak_source": f"{peaks_kind} hbm copy",
+                **common}
+    elif dom == "tcgen05":
+        ach = d["flops"] / secs / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": p_tc / 1e12, "unit": "TFLOP/s", "frac": ach * 1e12 / p_tc,
+                "traffic": None, "peak_source": f"{peaks_kind} bf16 sustained", **common}
+    else:
+        ach = d["flops"] / secs / 1e12
+        roof = {"bound": "simt", "achieved": ach, "peak": p_simt / 1e12, "unit": "TFLOP/s",
+                "frac": ach * 1e12 / p_simt, "traffic": None, "peak_source": "nominal SIMT", **common}
+    if dom == "tcgen05":
+        roof["kernel"] = "tcgen05 contraction steps (GEMM plus its scale / slice pre-passes)"
+        roof["algorithmic_tflops"] = d["flops"] / secs / 1e12
+        if prec_name in TENSOR_OPS_PER_FLOP:
+            r = TENSOR_OPS_PER_FLOP[prec_name]
+            roof.update({"tensor_ops_per_algorithmic_flop": r, "tensor_work_tflops": roof["algorithmic_tflops"] * r,
+                         "tensor_work_frac": roof["algorithmic_tflops"] * r * 1e12 / p_tc})
+        if prec_name == "ozaki":
+            roof["traffic"] = d["bytes"] / d["launches_per_run"] * OZ_CLASS_TRAFFIC_RATIO
+            roof["traffic_unit"] = "bytes per launch"
+            roof["traffic_source"] = OZ_CLASS_TRAFFIC_SOURCE
+    return roof, info, overall
 
 
 if __name__ == "__main__":

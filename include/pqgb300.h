@@ -325,6 +325,19 @@ int pq_mlp_train(pq_mlp* m, const float* X, const float* y, int64_t n, int epoch
  * activations (FP32 accumulation). */
 int pq_mlp_predict(pq_mlp* m, const float* X, int64_t n, float* out, int bf16);
 
+/* ---- diagnostics ----------------------------------------------------------
+ * Exercises the error path of the tensor-core kernels' bounded waits: one
+ * thread waits on a shared-memory mbarrier that nobody arrives at, for at
+ * most `polls` polls (1..2^20), records the expiry in the context's status
+ * word exactly as an expired wait in pq_tc.cu / pq_oz.cu does, and returns
+ * (no copies, MMAs or TMEM in flight).  *expired = 1 when the wait ran out.
+ * The call itself returns PQ_OK; the context's next synchronising call
+ * (pq_ctx_sync, a load, a plan run) returns PQ_ERR_DEVICE once and clears
+ * the status word, after which the context works normally.  Replaces the
+ * reference's failure behaviour for a missing or bad device result
+ * (src/backends/interactive.jl:44-49: an error, no process exit). */
+int pq_selftest_wait_expiry(pq_ctx* ctx, uint32_t polls, int* expired);
+
 #ifdef __cplusplus
 }
 #endif

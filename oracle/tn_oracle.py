@@ -814,6 +814,45 @@ def execute_ssa_plan(leaves, leaf_labels, steps, out_labels=()):
     return res
 
 
+def network_leaves(net: TensorNetworkCircuit):
+    """The network's current nodes as SSA leaves: (node names in node order,
+    arrays, integer labels, label extents, label of each index name).
+    Integer labels are numbered by first appearance over the nodes in order,
+    so an SSA pair plan over the same network's node order (a compiled
+    plan's ``steps``) applies to these leaves unchanged."""
+    names = list(net.nodes.keys())
+    label_of: dict[str, int] = {}
+    dims: list[int] = []
+    arrays, labels = [], []
+    for nl in names:
+        node = net.nodes[nl]
+        a = np.asarray(net.backend.load_tensor_data(node.data_label), dtype=CDT)
+        if a.ndim != len(node.indices):
+            raise ValueError(f"node {nl}: array rank {a.ndim} != {len(node.indices)} indices")
+        lab = []
+        for idx, d in zip(node.indices, a.shape):
+            if idx not in label_of:
+                label_of[idx] = len(dims)
+                dims.append(int(d))
+            elif dims[label_of[idx]] != int(d):
+                raise ValueError(f"index {idx} has extents {dims[label_of[idx]]} and {d}")
+            lab.append(label_of[idx])
+        arrays.append(a)
+        labels.append(lab)
+    return names, arrays, labels, dims, label_of
+
+
+def contract_along_steps(net: TensorNetworkCircuit, steps, out_edges=()):
+    """Contract the whole network along SSA ``steps`` over its node order
+    (the pair-plan execution of src/layer2.jl:294-321, each pair a
+    ``tensordot`` as src/layer1.jl:85-92); the result's modes follow
+    ``out_edges`` (index names).  Returns the complex128 result array."""
+    names, arrays, labels, dims, label_of = network_leaves(net)
+    if len(steps) != 2 * (len(names) - 1):
+        raise ValueError(f"{len(steps) // 2} steps for {len(names)} leaves")
+    return execute_ssa_plan(arrays, labels, list(steps), [label_of[e] for e in out_edges])
+
+
 def slice_leaves(leaves, leaf_labels, sliced, dims, s):
     """Leaves with the sliced labels fixed to the mixed-radix digits of slice
     ``s`` (first sliced label fastest); the fixed modes are removed."""
@@ -827,6 +866,13 @@ def slice_leaves(leaves, leaf_labels, sliced, dims, s):
         out.append(np.asarray(t)[idx])
         labs.append([x for x in l if x not in vals])
     return out, labs
+
+
+def random_bitstrings(n_qubits, count, seed):
+    """Seeded uniform random output bitstrings (character i = qubit i+1)."""
+    rng = np.random.default_rng(seed)
+    bits = rng.integers(0, 2, size=(count, n_qubits))
+    return ["".join("1" if b else "0" for b in row) for row in bits]
 
 
 def amplitude_index(bitstring):

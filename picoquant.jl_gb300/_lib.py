@@ -107,6 +107,7 @@ SIGNATURES = [
     ("pq_mlp_gradients", C.c_int, [vp, f32p, f32p, C.c_int64, f32p, f32p]),
     ("pq_mlp_train", C.c_int, [vp, f32p, f32p, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, f32p]),
     ("pq_mlp_predict", C.c_int, [vp, f32p, C.c_int64, f32p, C.c_int]),
+    ("pq_selftest_wait_expiry", C.c_int, [vp, C.c_uint32, C.POINTER(C.c_int)]),
 ]
 
 # exported by the library but optional for older builds

@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   }
-  if (!ok && status) atomicExch(status, kStatusTcTimeout);
+  if (!ok) report_timeout(status);
   fence_before();
   __syncthreads();
   if (warp == 1) {

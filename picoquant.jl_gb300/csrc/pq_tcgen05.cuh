@@ -42,9 +42,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// Bounded wait for the phase of the given parity; false when it expired.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+// Bounded wait for the phase of the given parity: at most `limit` polls;
+// false when it expired.
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -54,6 +55,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (ok) return true;
   }
   return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  return mbar_wait_polls(bar, parity, kWaitLimit);
+}
+// Records an expired wait in the context's status word (read by the host at
+// the next synchronising call, where it becomes PQ_ERR_DEVICE).
+__device__ __forceinline__ void report_timeout(int* status) {
+  if (status) atomicExch(status, kStatusTcTimeout);
 }
 // 1D bulk copy global -> shared (16-byte aligned addresses, size a multiple
 // of 16), completing as transaction bytes on `bar`.

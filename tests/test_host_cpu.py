@@ -2,6 +2,7 @@
 the native planners produce valid plans, and the product's graph layer (run
 over a numpy test backend) reproduces the oracle's bookkeeping."""
 import re
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -397,9 +398,10 @@ def test_randomized_sweep_orders(pq, O, host_backend):
 
 def test_bench_roofline_classes():
     """The bench's roofline assembly over per-step timings: every kernel class
-    (generic, SIMT GEMM, tcgen05, copy, skinny) is named, shares add up, and
-    the dominant class decides the bound (HBM for the skinny class, tensor
-    for tcgen05, with the exact scheme's tensor work per algorithmic flop)."""
+    (generic, SIMT GEMM, tcgen05, copy, skinny) is named, shares add up, each
+    step's lower bound is max(bytes / HBM, flops / peak), and the dominant
+    class's bound is the side with the larger summed lower bound (HBM for a
+    skinny class and for a shallow tensor-core pair, tensor for a deep one)."""
     import bench
 
     peaks = {"hbm_gbs": 6757.5, "bf16_tflops": 1871.0, "bf16_tflops_sustained": 1683.9}
@@ -410,13 +412,90 @@ def test_bench_roofline_classes():
     steps = [(0.2, False, feats(0, 10, 2, 1e6)), (3.0, False, feats(4, 28, 4, 4e9)),
              (0.1, True, feats(3, 12, 0, 1e5)), (0.5, False, feats(1, 20, 8, 1e8))]
     ms, batched, fs = zip(*steps)
-    roof, info = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki")
+    roof, info, overall = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki", 5.0)
     assert set(info) == {"generic", "skinny", "copy", "gemm_simt"}
     assert abs(sum(d["share"] for d in info.values()) - 1.0) < 1e-12
     assert roof["bound"] == "hbm" and roof["kernel"] == "skinny" and roof["unit"] == "GB/s"
     assert abs(roof["achieved"] - 4e9 / 3e-3 / 1e9) < 1e-6 and roof["frac"] == roof["achieved"] / 6757.5
+    assert abs(info["skinny"]["lower_bound_ms"] - 1e3 * 4e9 / 6757.5e9) < 1e-9
+    assert overall["wall_ms"] == 5.0 and 0 < overall["frac_of_wall"] < 1
+    # a shallow tensor-core pair (K = 2^8): its bytes bound it
     steps.append((9.0, False, feats(2, 28, 8, 5e9)))
     ms, batched, fs = zip(*steps)
-    roof, info = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki")
-    assert roof["bound"] == "tensor" and roof["tensor_ops_per_algorithmic_flop"] == 15.0
-    assert abs(roof["achieved"] - 8.0 * 2 ** 28 * 2 ** 8 / 9e-3 / 1e12) < 1e-9
+    roof, info, _ = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki", 13.0)
+    assert roof["bound"] == "hbm" and roof["tensor_ops_per_algorithmic_flop"] == 15.0
+    assert abs(roof["achieved"] - 5e9 / 9e-3 / 1e9) < 1e-6
+    assert abs(roof["algorithmic_tflops"] - 8.0 * 2 ** 28 * 2 ** 8 / 9e-3 / 1e12) < 1e-9
+    # a deep one (K = 2^12): its flops bound it
+    steps[-1] = (9.0, False, feats(2, 28, 12, 5e9))
+    ms, batched, fs = zip(*steps)
+    roof, info, _ = bench.roofline_from_profile(ms, batched, fs, peaks, "measured", 4, "ozaki", 13.0)
+    assert roof["bound"] == "tensor" and roof["unit"] == "TFLOP/s"
+    assert abs(roof["achieved"] - 8.0 * 2 ** 28 * 2 ** 12 / 9e-3 / 1e12) < 1e-9
+    lb = 1e3 * 8.0 * 2 ** 40 / 1683.9e12
+    assert abs(info["tcgen05"]["lower_bound_ms"] - lb) < 1e-9
+
+
+def test_reference_arm_loads_no_product_library():
+    """bench.py's CPU reference arm runs the FP64 oracle only: in a fresh
+    process it neither imports the product package nor maps its library."""
+    import json
+    import subprocess
+    import sys
+
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'grid4x5_d12_amps', "
+            "'--steps', '1']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED', int('libpqgb300' in maps), int('pqgb300' in sys.modules), int('torch' in sys.modules))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=str(ROOT), capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["cpu_baseline"]["sample"].startswith("timed")
+    assert lines[-1] == "LOADED 0 0 0"
+
+
+def test_recorded_plan_matches_oracle_network():
+    """The committed 6x6 depth-16 plan record applies to the network the
+    oracle builds itself (same leaves, same index names, in order), and its
+    steps form one whole contraction of it."""
+    import json
+
+    import bench
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import tn_oracle as O
+
+    rec = json.loads(bench.PLAN_FILE.read_text())
+    net = bench.oracle_network(O, rec)
+    assert len(rec["steps"]) == 2 * (len(net.nodes) - 1)
+    assert 39.0 < rec["log2_cmacs"] < 40.0 and rec["log2_max_elems"] <= 28.0
+    seen = set()
+    for i, s in enumerate(rec["steps"]):
+        assert s < len(net.nodes) + i // 2 and s not in seen
+        seen.add(s)
+
+
+def test_oracle_amplitude_along_plan_record(pq, O):
+    """The bench's oracle pin on a small circuit: a plan record made from the
+    product's planner, replayed on the oracle's own network, gives the
+    state-vector amplitude."""
+    import bench
+
+    rows, cols, depth = 3, 3, 8
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
+    bits = pq.random_bitstrings(n, 1, seed=2027)[0]
+    net = pq.build_network(n, gates, decompose=True, backend=bench._HostStore())
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    steps, cm, mx, name = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    nodes = list(net.nodes.keys())
+    rec = {"rows": rows, "cols": cols, "depth": depth, "circuit_seed": 2026, "bitstring": bits, "leaves": nodes,
+           "leaf_indices": [list(net.nodes[x].indices) for x in nodes], "steps": steps}
+    amp, secs = bench.oracle_amplitude(O, rec)
+    ref = O.statevector(n, O.random_grid_gates(rows, cols, depth, seed=2026))[O.amplitude_index(bits)]
+    assert abs(amp - ref) < 1e-12 * max(1.0, abs(ref)) and secs >= 0
+    rec["leaves"] = nodes[1:] + nodes[:1]
+    with pytest.raises(RuntimeError):
+        bench.oracle_network(O, rec)

@@ -60,3 +60,35 @@ def test_noalloc_gather_rejects_oversize_request(pq):
     # still usable afterwards
     assert np.array_equal(_gather(be, "pq_gather_elements_noalloc", "v", [0, 7], np.complex128), [1, 1])
     be.close()
+
+
+def test_noalloc_gather_allocates_nothing(pq):
+    """The property the entry point exists for: the context's device memory
+    in use is the same before and after each call, and with the context's
+    memory cap set to exactly what is in use (so any further allocation
+    fails) the allocating gather is refused with PQ_ERR_OOM while the
+    allocation-free one still returns the right values, twice in a row."""
+    from pqgb300 import _lib as L
+
+    be = pq.GB300Backend(pq.PREC_C64)
+    rng = np.random.default_rng(11)
+    psi = rng.standard_normal(1 << 18) + 1j * rng.standard_normal(1 << 18)
+    be.save_tensor_data("psi", psi.reshape((2,) * 18, order="F"))
+    used = be.mem_in_use()
+    assert used > 0
+    for n in (4096, MAX_ELEMS):
+        idx = rng.integers(0, psi.size, n)
+        got = _gather(be, "pq_gather_elements_noalloc", "psi", idx, np.complex128)
+        assert be.mem_in_use() == used
+        assert np.max(np.abs(got - psi[idx])) <= 2e-6 * np.max(np.abs(psi))
+    be.set_mem_cap(used)
+    idx = rng.integers(0, psi.size, 1000)
+    with pytest.raises(L.PQError) as e:
+        _gather(be, "pq_gather_elements", "psi", idx, np.complex128)
+    assert e.value.code == L.PQ_ERR_OOM
+    for _ in range(2):
+        got = _gather(be, "pq_gather_elements_noalloc", "psi", idx, np.complex64)
+        assert be.mem_in_use() == used
+        assert np.max(np.abs(got - psi[idx])) <= 2e-6 * np.max(np.abs(psi))
+    be.set_mem_cap(0)
+    be.close()
