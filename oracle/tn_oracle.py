@@ -226,6 +226,38 @@ class TensorNetworkCircuit:
         return f"{s}_{self.counters[s]}"
 
 
+def network_from_dict(d, backend=None):
+    """src/layer3.jl:654-681 (``network_from_dict``): edges and nodes in the
+    file's order, label counters continued after the largest numbers
+    present.  Also reads the older form of the reference's example networks
+    (examples/ghz_3.json), whose nodes embed their tensor (``data_re``,
+    ``data_im`` flattened column-major, ``data_dims``; the node name is its
+    data label) and whose edges carry only src/dst."""
+    net = TensorNetworkCircuit(int(d["number_qubits"]), backend)
+    net.edges = OrderedDict()
+    index = 0
+    for k, v in d["edges"].items():
+        index = max(index, int(k.split("_")[-1]))
+        net.edges[k] = Edge(v["src"], v["dst"], v.get("qubit"), bool(v.get("virtual", False)))
+    net.nodes = OrderedDict()
+    node = 0
+    for k, v in d["nodes"].items():
+        node = max(node, int(k.split("_")[-1]))
+        if "data_re" in v:
+            dims = [int(x) for x in v["data_dims"]]
+            data = (np.asarray(v["data_re"], dtype=np.float64) + 1j * np.asarray(v["data_im"], dtype=np.float64))
+            net.backend.save_tensor_data(k, data.reshape(dims, order="F"))
+            net.nodes[k] = Node([str(x) for x in v["indices"]], dims, k)
+        else:
+            net.nodes[k] = Node([str(x) for x in v["indices"]], [int(x) for x in v["dims"]], str(v["data_label"]))
+    net.input_qubits = [str(x) for x in d["input_qubits"]]
+    net.output_qubits = [str(x) for x in d["output_qubits"]]
+    net.qubit_ordering = [int(x) for x in d.get("qubit_ordering", range(1, net.number_qubits + 1))]
+    net.node_layers = {str(k): int(v) for k, v in d.get("node_layers", {}).items()}
+    net.counters = {"index": index, "node": node, "layer": max([0, *net.node_layers.values()])}
+    return net
+
+
 def decompose_gate(gate_data, threshold=1e-15):
     """src/layer3.jl:715-739: SVD split over positions (1,3) | (2,4)."""
     dims = gate_data.shape

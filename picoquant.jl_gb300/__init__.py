@@ -10,11 +10,13 @@ backend (the role of ``InteractiveBackend{T}``).  All numeric work runs in
 from ._lib import (PQ_C64, PQ_C128, PQError, PREC_3XBF16, PREC_3XTF32, PREC_6XTF32, PREC_C64, PREC_C128, PREC_OZAKI)
 from .backend import GB300Backend, Metrics, decompose_array, record_compute_costs, record_memory_costs
 from .dsl import DSLBackend, DSLPlan, compile_dsl, execute_dsl_file
-from .mps import (MPSState, calculate_mps_amplitudes, compress_bond, contract_mps_tensor_network_circuit,
+from .mps import (MPSState, calculate_mps_amplitudes, compress_bond, compress_tensor_chain,
+                  contract_mps_tensor_network_circuit,
                   contract_tensor_network_circuit_with_compression)
 from .circuits import (CX, CZ, SWAP, H, build_network, cphase, ghz_gates, grid_patterns, grid_shape, haar_su2,
                        operator_to_tensor, qft_gates, random_bitstrings, random_grid_gates)
 from .contraction import (contract_network, contract_pair, create_ncon_indices, full_wavefunction_contraction,
+                          inorder_contraction, merge_common_bonds,
                           multi_index_partition, partition_network_on_virtual_bonds, random_contraction_plan,
                           replace_with_view, slice_tensor_network, sort_indices)
 from .network import (Edge, Node, TensorNetworkCircuit, add_gate, add_input, add_output, decompose_gate,

@@ -61,6 +61,68 @@ def contract_pair(network, A_label, B_label=None):
     return C_label
 
 
+def merge_common_bonds(network, a_label, b_label):
+    """src/layer2.jl:25-71: when two nodes share more than one index, move
+    the shared indices last in both tensors (``permute_tensor``) and merge
+    them into one new virtual index (``reshape_tensor``, column-major, no
+    data move beyond the permutation), replacing the shared edges by one.
+    Both tensors order their shared indices as ``a`` holds them (the
+    reference orders each by its own index order, which pairs the wrong
+    elements when the two orders differ; where they agree the result is the
+    same)."""
+    from .network import Edge
+
+    a, b = network.nodes[a_label], network.nodes[b_label]
+    common = [x for x in a.indices if x in b.indices]
+    if len(common) <= 1:
+        return
+    a_common = [k for k, x in enumerate(a.indices) if x in b.indices]
+    a_rest = [k for k, x in enumerate(a.indices) if x not in b.indices]
+    b_common = [b.indices.index(x) for x in common]
+    b_rest = [k for k, x in enumerate(b.indices) if x not in a.indices]
+    permute_tensor(network, a_label, [k + 1 for k in a_rest + a_common])
+    permute_tensor(network, b_label, [k + 1 for k in b_rest + b_common])
+    new_edge = new_label(network, "index")
+    dim = int(np.prod([a.dims[k] for k in a_common]))
+    dims_a = dict(zip(a.indices, a.dims))
+    dims_b = dict(zip(b.indices, b.dims))
+    idx_a = [a.indices[k] for k in a_rest] + [new_edge]
+    idx_b = [b.indices[k] for k in b_rest] + [new_edge]
+    network.nodes[a_label] = Node(idx_a, [dims_a[x] for x in idx_a[:-1]] + [dim], a_label)
+    network.nodes[b_label] = Node(idx_b, [dims_b[x] for x in idx_b[:-1]] + [dim], b_label)
+    for lab, rest, com in ((a_label, a_rest, a_common), (b_label, b_rest, b_common)):
+        l, m = len(rest), len(com)
+        reshape_tensor(network, lab, [[k] for k in range(1, l + 1)] + [list(range(l + 1, l + m + 1))])
+    network.edges[new_edge] = Edge(a_label, b_label, None, True)
+    for e in common:
+        del network.edges[e]
+
+
+def inorder_contraction(network):
+    """src/layer2.jl:78-112: contract the network layer by layer from the
+    inputs: every node of a gate layer (then of the output layer) absorbs its
+    distinct in-neighbours, then each pair of the layer's new nodes (``y >
+    x`` by name, x varying fastest) has its shared bonds merged."""
+    from .network import inneighbours
+
+    groups: dict[int, list] = {}
+    for k, v in network.node_layers.items():
+        groups.setdefault(v, []).append(k)
+    layers = [k for k in sorted(groups) if k > 0]
+    if -1 in groups:
+        layers.append(-1)
+    for layer in layers:
+        new_nodes = []
+        for node in groups[layer]:
+            for in_node in list(dict.fromkeys(inneighbours(network, node))):
+                node = contract_pair(network, in_node, node)
+            new_nodes.append(node)
+        for y in new_nodes:
+            for x in new_nodes:
+                if y > x:
+                    merge_common_bonds(network, x, y)
+
+
 def layer_order(network):
     """Nodes grouped by layer, gate layers ascending then the output layer
     (src/layer2.jl:149-161)."""

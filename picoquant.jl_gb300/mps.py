@@ -62,6 +62,18 @@ def compress_bond(network, node_1, node_2, threshold=1e-13, max_rank=0):
                             max_rank=max_rank, left_label=node_1, right_label=node_2)
 
 
+def compress_tensor_chain(network, nodes, threshold=1e-13, max_rank=0):
+    """src/layer2.jl:423-450: compress the bonds of a chain of tensors with a
+    forward then a backward sweep of ``compress_bond`` over consecutive
+    pairs (singular values below ``threshold`` and beyond ``max_rank``,
+    0 = unbounded, are dropped).  The chain's tensors must be joined only
+    to their neighbours by virtual bonds."""
+    for i in range(len(nodes) - 1):
+        compress_bond(network, nodes[i], nodes[i + 1], threshold=threshold, max_rank=max_rank)
+    for i in range(len(nodes) - 2, -1, -1):
+        compress_bond(network, nodes[i], nodes[i + 1], threshold=threshold, max_rank=max_rank)
+
+
 def _gate_layers(network):
     layers: dict[int, list] = {}
     for k, v in network.node_layers.items():
@@ -139,24 +151,36 @@ def calculate_mps_amplitudes(network, mps_nodes, result="result"):
 
 class MPSState:
     """src/mps.jl:9-110: amplitudes read from an MPS without forming the
-    state: per qubit the two slices (bit 0 / 1) of its tensor, contracted
-    along the chain for a requested bitstring (host FP64)."""
+    state.  Each qubit's tensor is copied once, in the backend, with its
+    output index moved first (the reference keeps the same per-qubit data on
+    the host); an amplitude takes each copy's slab for the requested bit
+    (``view_tensor``) and contracts the slabs along the chain with the
+    backend's ``contract_tensors`` (on the device for the GB300 backend), in
+    the reference's order and with its ncon labels."""
+
+    _next_uid = 0
 
     def __init__(self, network, mps_nodes):
         n = len(mps_nodes)
         self.n = n
-        self.nodes, self.data = [], []
+        self.backend = network.backend
+        MPSState._next_uid += 1
+        self._tag = f"__mpsstate{MPSState._next_uid}"
+        self.nodes, self.site = [], []
         outs = set(network.output_qubits)
         positions = []
+        be = self.backend
         for i, nl in enumerate(mps_nodes):
             node = network.nodes[nl]
             p = next(k for k, x in enumerate(node.indices) if x in outs)
             positions.append(p)
             other = [k for k in range(len(node.indices)) if k != p]
-            t = np.asarray(network.backend.load_tensor_data(nl), dtype=np.complex128)
-            t = np.transpose(t, [p] + other)
+            lab = f"{self._tag}_site{i + 1}"
+            # copy (a view over the whole first mode), then the output index first
+            be.view_tensor(lab, node.data_label, 1, range(1, node.dims[0] + 1))
+            be.permute_tensor(lab, [p + 1] + [k + 1 for k in other])
+            self.site.append(lab)
             self.nodes.append(Node([node.indices[k] for k in other], [node.dims[k] for k in other], f"n_{i + 1}"))
-            self.data.append([t[0], t[1]])
         self.ordering = [0] * n
         for i, e in zip(range(n), network.qubit_ordering):
             self.ordering[e - 1] = i
@@ -167,6 +191,17 @@ class MPSState:
     def __len__(self):
         return 2 ** self.n
 
+    def _slab(self, i, bit):
+        """Site i's slab for output value ``bit`` as a tensor over its other
+        indices: a width-1 view of the output mode, that unit mode then
+        merged into its neighbour (a reshape, no data move)."""
+        lab = f"{self._tag}_slab{i + 1}"
+        self.backend.view_tensor(lab, self.site[i], 1, range(bit + 1, bit + 2))
+        r = len(self.nodes[i].indices)
+        groups = [[1, 2]] + [[k] for k in range(3, r + 2)] if r else [[1]]
+        self.backend.reshape_tensor(lab, groups)
+        return lab
+
     def __getitem__(self, conf):
         """``state["0110"]`` (character i is the output of qubit
         ``qubit_ordering[i]``) or ``state[(1, 2, 2, 1)]`` (1-based values as
@@ -175,15 +210,24 @@ class MPSState:
             bits = [1 if ch == "1" else 0 for ch in conf]
         else:
             bits = [(int(x) - 1) for x in conf]
+        be = self.backend
         n1 = self.nodes[0]
-        d1 = self.data[0][bits[self.ordering[0]]]
+        cur = self._slab(0, bits[self.ordering[0]])
         for idx in range(1, self.n):
             n2 = self.nodes[idx]
             common, remaining = sort_indices(n1, n2)
             ia, ib = create_ncon_indices(n1, n2, common, remaining)
-            d2 = self.data[idx][bits[self.ordering[idx]]]
-            ca = [k for k, x in enumerate(ia) if x > 0]
-            cb = [ib.index(ia[k]) for k in ca]
-            d1 = np.tensordot(d1, d2, axes=(ca, cb))
+            nxt = self._slab(idx, bits[self.ordering[idx]])
+            out = f"{self._tag}_chain{idx}"
+            be.contract_tensors(cur, ia, nxt, ib, out)  # consumes both slabs
+            cur = out
             n1 = Node(list(remaining), [1] * len(remaining), "n1")
-        return complex(np.asarray(d1).reshape(-1)[0])
+        v = be.load_tensor_data(cur)
+        be.delete_tensor(cur)
+        return complex(np.asarray(v).reshape(-1)[0])
+
+    def close(self):
+        """Release the per-qubit copies held in the backend."""
+        for lab in self.site:
+            self.backend.delete_tensor(lab)
+        self.site = []

@@ -261,8 +261,9 @@ def edge_to_dict(edge: Edge) -> dict:
 
 
 def edge_from_dict(d) -> Edge:
-    """src/layer3.jl:594-599."""
-    return Edge(d["src"], d["dst"], d["qubit"], d["virtual"])
+    """src/layer3.jl:594-599 (``qubit`` / ``virtual`` optional, as in the
+    older example files that carry only src/dst)."""
+    return Edge(d["src"], d["dst"], d.get("qubit"), bool(d.get("virtual", False)))
 
 
 def node_to_dict(node: Node) -> dict:
@@ -276,12 +277,25 @@ def node_from_dict(d) -> Node:
     return Node([str(x) for x in d["indices"]], [int(x) for x in d["dims"]], str(d["data_label"]))
 
 
-def to_dict(network: TensorNetworkCircuit) -> dict:
-    """src/layer3.jl:630-647 (key order kept)."""
+def to_dict(network: TensorNetworkCircuit, with_data: bool = False) -> dict:
+    """src/layer3.jl:630-647 (key order kept).  ``with_data`` also embeds each
+    node's tensor as the reference's example networks do (``data_re``,
+    ``data_im`` flattened column-major, ``data_dims``), read back from the
+    backend, so the file carries everything needed to contract it
+    elsewhere."""
+    nodes = {}
+    for k, v in network.nodes.items():
+        nd = node_to_dict(v)
+        if with_data:
+            a = np.asarray(network.backend.load_tensor_data(v.data_label), dtype=np.complex128)
+            flat = a.reshape(-1, order="F")
+            nd.update({"data_re": flat.real.tolist(), "data_im": flat.imag.tolist(),
+                       "data_dims": [int(x) for x in a.shape]})
+        nodes[str(k)] = nd
     return {
         "number_qubits": network.number_qubits,
         "edges": {str(k): edge_to_dict(v) for k, v in network.edges.items()},
-        "nodes": {str(k): node_to_dict(v) for k, v in network.nodes.items()},
+        "nodes": nodes,
         "input_qubits": [str(x) for x in network.input_qubits],
         "output_qubits": [str(x) for x in network.output_qubits],
         "qubit_ordering": [int(x) for x in network.qubit_ordering],
@@ -290,9 +304,14 @@ def to_dict(network: TensorNetworkCircuit) -> dict:
 
 
 def network_from_dict(d, backend=None) -> TensorNetworkCircuit:
-    """src/layer3.jl:654-681: the graph of ``d`` on ``backend`` (whose tensor
-    store must hold the nodes' data labels); the label counters continue
-    after the largest node and index numbers present."""
+    """src/layer3.jl:654-681: the graph of ``d`` on ``backend``; the label
+    counters continue after the largest node and index numbers present.
+    Nodes that embed their tensor (``data_re``, ``data_im``, ``data_dims``,
+    as written by ``to_dict(..., with_data=True)`` and as in the reference's
+    example networks, examples/ghz_3.json) are uploaded to the backend under
+    the node's name; the others refer by ``data_label`` to tensors the
+    backend already holds.  Files without ``qubit_ordering`` /
+    ``node_layers`` get the identity ordering and no layers."""
     net = TensorNetworkCircuit(int(d["number_qubits"]), backend)
     net.edges = {}
     index = 0
@@ -303,20 +322,26 @@ def network_from_dict(d, backend=None) -> TensorNetworkCircuit:
     node = 0
     for k, v in d["nodes"].items():
         node = max(node, int(k.split("_")[-1]))
-        net.nodes[k] = node_from_dict(v)
+        if "data_re" in v:
+            dims = [int(x) for x in v["data_dims"]]
+            data = np.asarray(v["data_re"], dtype=np.float64) + 1j * np.asarray(v["data_im"], dtype=np.float64)
+            net.nodes[k] = Node([str(x) for x in v["indices"]], dims, k)
+            save_tensor_data(net, k, data.reshape(dims, order="F"))
+        else:
+            net.nodes[k] = node_from_dict(v)
     net.input_qubits = [str(x) for x in d["input_qubits"]]
     net.output_qubits = [str(x) for x in d["output_qubits"]]
-    net.qubit_ordering = [int(x) for x in d["qubit_ordering"]]
-    net.node_layers = {str(k): int(v) for k, v in d["node_layers"].items()}
+    net.qubit_ordering = [int(x) for x in d.get("qubit_ordering", range(1, net.number_qubits + 1))]
+    net.node_layers = {str(k): int(v) for k, v in d.get("node_layers", {}).items()}
     net.counters = {"index": index, "node": node, "layer": max([0, *net.node_layers.values()])}
     return net
 
 
-def to_json(network: TensorNetworkCircuit, indent: int = 0) -> str:
-    """src/layer3.jl:688-695."""
+def to_json(network: TensorNetworkCircuit, indent: int = 0, with_data: bool = False) -> str:
+    """src/layer3.jl:688-695 (``with_data`` as in ``to_dict``)."""
     import json
 
-    return json.dumps(to_dict(network), indent=indent if indent else None)
+    return json.dumps(to_dict(network, with_data), indent=indent if indent else None)
 
 
 def network_from_json(json_str: str, backend=None) -> TensorNetworkCircuit:

@@ -136,3 +136,53 @@ def test_random_grid_full_wavefunction(pq, O, prec, shape):
     pq.full_wavefunction_contraction(net, "vector")
     assert rel(pq.load_tensor_data(net, "result"), O.statevector(n, g)) < TOL[prec]
     be.close()
+
+
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "reference_examples"
+
+
+def test_reference_json_network_edge_plan(pq, prec):
+    """A network produced by the reference (examples/ghz_3.json, copied in
+    tests/golden), loaded through network_from_json onto the GB300 backend
+    and contracted along the reference's edge plan (ghz_3_plan.json), gives
+    the reference's own contracted network (ghz_3_contracted.json): node
+    name, index order and data."""
+    import json
+
+    be = pq.GB300Backend(prec)
+    net = pq.network_from_json((GOLDEN / "ghz_3.json").read_text(), be)
+    for e in json.loads((GOLDEN / "ghz_3_plan.json").read_text()):
+        pq.contract_pair(net, e)
+    want = json.loads((GOLDEN / "ghz_3_contracted.json").read_text())
+    assert list(net.nodes) == ["node_5"] and list(net.edges) == list(want["edges"])
+    w = want["nodes"]["node_5"]
+    assert net.nodes["node_5"].indices == w["indices"]
+    got = np.asarray(be.load_tensor_data("node_5")).reshape(-1, order="F")
+    ref = np.asarray(w["data_re"]) + 1j * np.asarray(w["data_im"])
+    assert np.max(np.abs(got - ref)) <= TOL[prec]
+    be.close()
+
+
+def test_json_round_trip_contracts_on_gpu(pq, O, prec):
+    """A random circuit's network written with its data (to_json with
+    with_data=True), read back onto a fresh GB300 backend and contracted by
+    a compiled plan, gives the oracle's amplitude of the original circuit."""
+    n = 12
+    gates = pq.random_grid_gates(3, 4, 8, seed=5)
+    bits = pq.random_bitstrings(n, 1, seed=6)[0]
+    be0 = pq.GB300Backend(pq.PREC_C128)
+    net0 = pq.build_network(n, gates, decompose=True, backend=be0)
+    pq.add_input(net0, "0" * n)
+    pq.add_output(net0, bits)
+    text = pq.to_json(net0, with_data=True)
+    be0.close()
+    be = pq.GB300Backend(prec)
+    net = pq.network_from_json(text, be)
+    steps, _, _, _ = pq.planning.best_flop_plan(net, out_edges=[])
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    plan.execute()
+    amp = complex(np.asarray(plan.result()).reshape(-1)[0])
+    plan.close()
+    ref = O.statevector(n, O.random_grid_gates(3, 4, 8, seed=5))[O.amplitude_index(bits)]
+    assert abs(amp - ref) <= TOL[prec] * 2.0 ** (-n / 2) * 8
+    be.close()

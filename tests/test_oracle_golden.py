@@ -140,15 +140,15 @@ def test_multi_index_partition(O):
     assert O.multi_index_partition((2, 3, 2), 6, 6) == (2, 3)
 
 
-QASM_DIR = Path("/root/reference/examples")
+GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_examples"
 
 
-@pytest.mark.skipif(not QASM_DIR.exists(), reason="reference checkout not present")
-@pytest.mark.parametrize("name,n", [("qft_2", 2), ("qft_3", 3), ("qft_5", 5), ("ghz_3", 3)])
+@pytest.mark.parametrize("name,n", [("qft_2", 2), ("qft_3", 3), ("qft_5", 5), ("qft_10", 10), ("ghz_3", 3)])
 def test_reference_qasm_fixtures(O, name, n):
-    # examples/*.qasm: transpiled QFT / GHZ circuits; on |0..0> the QFT gives the
-    # uniform state and GHZ gives (|0..0> + |1..1>)/sqrt(2).
-    gates = O.parse_qasm((QASM_DIR / f"{name}.qasm").read_text())
+    # examples/*.qasm of the reference (copies in tests/golden): transpiled QFT /
+    # GHZ circuits; on |0..0> the QFT gives the uniform state and GHZ gives
+    # (|0..0> + |1..1>)/sqrt(2).
+    gates = O.parse_qasm((GOLDEN / f"{name}.qasm").read_text())
     net = O.build_network(n, gates)
     O.add_input(net, "0" * n)
     O.full_wavefunction_contraction(net, "vector")
@@ -161,6 +161,30 @@ def test_reference_qasm_fixtures(O, name, n):
         ref = np.zeros(2**n)
         ref[0] = ref[-1] = 1 / math.sqrt(2)
         assert np.max(np.abs(np.abs(out) - ref)) < 1e-12
+
+
+def test_reference_edge_plan_golden(O):
+    """examples/ghz_3.json contracted along examples/ghz_3_plan.json (edges
+    index_4 then index_6, one contract_pair! each) gives the network the
+    reference wrote to examples/ghz_3_contracted.json: the node name
+    (node_5), its index order (symdiff of the operands' indices,
+    src/layer1.jl:89) and its data."""
+    import json
+
+    net = O.network_from_dict(json.loads((GOLDEN / "ghz_3.json").read_text()))
+    plan = json.loads((GOLDEN / "ghz_3_plan.json").read_text())
+    for e in plan:
+        O.contract_pair(net, e)
+    want = json.loads((GOLDEN / "ghz_3_contracted.json").read_text())
+    assert list(net.nodes) == list(want["nodes"]) == ["node_5"]
+    assert list(net.edges) == list(want["edges"])
+    for k, e in want["edges"].items():
+        assert (net.edges[k].src, net.edges[k].dst) == (e["src"], e["dst"])
+    w = want["nodes"]["node_5"]
+    assert net.nodes["node_5"].indices == w["indices"] and net.nodes["node_5"].dims == w["data_dims"]
+    got = np.asarray(net.backend.load_tensor_data("node_5")).reshape(-1, order="F")
+    ref = np.asarray(w["data_re"]) + 1j * np.asarray(w["data_im"])
+    assert np.max(np.abs(got - ref)) < 1e-15
 
 
 def test_mlp_oracle_gradient_finite_differences():
