@@ -110,10 +110,13 @@ SWEEP_RANDOM = 64
 
 
 def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026, rank=0, target=28.0,
-                 planner="learned", steps=None):
+                 planner="learned", steps=None, tuning="off"):
     """The sliced single-amplitude workload on a new backend of ``precision``:
     network, plan (``steps`` if given, else the named planner's choice) and
-    the sliced bonds chosen for a 2^target-element intermediate limit."""
+    the sliced bonds chosen for a 2^target-element intermediate limit.
+    ``tuning="cache"``: the autotuner's table for this GPU is loaded (the
+    plan's classes it lacks tuned and the cache written back) and the plan
+    compiled under it."""
     n = rows * cols
     gates = pq.random_grid_gates(rows, cols, depth, seed=seed)
     bits = pq.random_bitstrings(n, 1, seed=seed + 1 + rank)[0]
@@ -139,9 +142,23 @@ def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026
     plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
     sliced = plan.choose_slices(max_sliced=n_sliced, log2_target=target)
     t_plan = time.perf_counter() - t0
+    tune_info = None
+    if tuning == "cache":
+        from pqgb300 import autotune as AT
+
+        t1 = time.perf_counter()
+        loaded = AT.Tuner(be).load()
+        tuner, new = AT.ensure_tuned(be, [plan])
+        plan.close()
+        plan = pq.NetworkPlan(net, steps=steps, out_edges=[])  # compiled under the tuned table
+        tune_info = {"classes": len(tuner.entries), "cache_loaded": loaded, "tuned_now": new,
+                     "seconds": time.perf_counter() - t1, "cache": AT.cache_path().name,
+                     "changed": [{"key": k, "choice": AT.choice_name(e["choice"]),
+                                  "default": AT.choice_name(e["default"]), "ms": e["ms"]}
+                                 for k, e in tuner.entries.items() if e["choice"] != e["default"]]}
     return dict(be=be, net=net, plan=plan, sliced=sliced, gates=gates, bits=bits, cmacs=cm, max_elems=mx,
                 planner=name, t_plan=t_plan, n=n, rows=rows, cols=cols, depth=depth, seed=seed,
-                bits_seed=seed + 1 + rank)
+                bits_seed=seed + 1 + rank, tuning=tune_info)
 
 
 # The 6x6 depth-16 plan the GB300 arm contracts, recorded for the CPU
@@ -239,6 +256,9 @@ def main():
     ap.add_argument("--oracle", default="full", choices=["full", "skip"],
                     help="contract the headline amplitude with the FP64 oracle too (rel_err_vs_oracle, cpu_baseline)")
     ap.add_argument("--write-plan", default="", help="write the sliced workload's plan record to this JSON file")
+    ap.add_argument("--tuning", default="cache", choices=["cache", "off"],
+                    help="cache: the autotuner's per-class kernel choices (cache for this GPU and kernels, missing "
+                         "classes of the plan tuned first, outside the timed region); off: the fixed rules")
     ap.add_argument("--slice-target", type=float, default=28.0,
                     help="log2 elements allowed per slice intermediate when choosing sliced bonds")
     ap.add_argument("--fp64", default="full", choices=["full", "skip"],
@@ -724,7 +744,8 @@ def run_gb300(args, world, rank):
 
     if args.workload == "grid6x6_d16_sliced":
         rows, cols, depth = args.rows, args.cols, args.depth
-        w = build_sliced(pq, precision, rows, cols, depth, rank=rank, target=args.slice_target)
+        w = build_sliced(pq, precision, rows, cols, depth, rank=rank, target=args.slice_target,
+                         tuning=args.tuning if precision != pq.PREC_C128 else "off")
         be, plan, sliced = w["be"], w["plan"], w["sliced"]
         if args.batch <= 0:
             args.batch = plan.auto_batch(sliced)
@@ -861,6 +882,7 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
             Path(args.write_plan).parent.mkdir(parents=True, exist_ok=True)
             Path(args.write_plan).write_text(json.dumps(rec))
         extra["amplitude"] = [float(np.real(result)), float(np.imag(result))]
+        extra["tuning"] = w.get("tuning")
         extra["plan"] = {"planner": w["planner"], "cmacs_unsliced": w["cmacs"], "max_elems_unsliced": w["max_elems"],
                          "sliced_bonds": len(sliced), "planning_s": w["t_plan"], "plan_sha": plan_sha(rec["steps"]),
                          "same_plan_as_reference_arm": bool(ref_rec is not None and ref_rec["steps"] == rec["steps"]

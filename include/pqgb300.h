@@ -325,6 +325,33 @@ int pq_mlp_train(pq_mlp* m, const float* X, const float* y, int64_t n, int epoch
  * activations (FP32 accumulation). */
 int pq_mlp_predict(pq_mlp* m, const float* X, int64_t n, float* out, int bf16);
 
+/* ---- autotuning -------------------------------------------------------------
+ * No counterpart in the reference, which leaves kernel choice to its array
+ * library (TensorOperations -> BLAS / cuTENSOR, src/layer1.jl:85-92).
+ * A pair's tuning class is a 64-bit key: the context's precision mode, the
+ * ceil-log2 of its M (A-side free), N (B-side free), K (contracted) and batch
+ * extents, and whether A's / B's unit-stride mode is contracted.  A choice is
+ * three ints: kernel class (0 generic, 1 SIMT GEMM, 2 tensor core, 4 skinny),
+ * tile width (16/32/64/128, 0 = default rule) and orientation (1 as given,
+ * 2 as C = B x A, 0 = default rule) of the exact-accumulation tensor-core
+ * class.
+ *
+ * pq_pair_tuning analyses C = symdiff(A, B) (A's a_rank labels and extents
+ * first, then B's) in the context's precision, ignoring its table: writes
+ * the key and every eligible choice (the default first; up to max_choices,
+ * 3 ints each) and their count.
+ * pq_ctx_set_tuning replaces the context's table with n (key, choice)
+ * entries; from then on contractions, compiled plans and measurements run
+ * a pair of a listed class with its choice (when eligible for that pair,
+ * else the default).  n = 0 clears it. */
+int pq_pair_tuning(pq_ctx* ctx, int a_rank, int b_rank, const int32_t* labels, const int64_t* dims,
+                   uint64_t* key, int max_choices, int32_t* choices, int* n_choices);
+int pq_ctx_set_tuning(pq_ctx* ctx, int n, const uint64_t* keys, const int32_t* choices);
+int pq_ctx_tuning_size(pq_ctx* ctx, int* n);
+/* The CUDA device's name (NUL-terminated, at most cap bytes), which keys the
+ * autotuner's persisted cache. */
+int pq_device_name(int device, char* out, int cap);
+
 /* ---- diagnostics ----------------------------------------------------------
  * Exercises the error path of the tensor-core kernels' bounded waits: one
  * thread waits on a shared-memory mbarrier that nobody arrives at, for at

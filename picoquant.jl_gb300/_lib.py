@@ -108,6 +108,11 @@ SIGNATURES = [
     ("pq_mlp_train", C.c_int, [vp, f32p, f32p, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, f32p]),
     ("pq_mlp_predict", C.c_int, [vp, f32p, C.c_int64, f32p, C.c_int]),
     ("pq_selftest_wait_expiry", C.c_int, [vp, C.c_uint32, C.POINTER(C.c_int)]),
+    ("pq_ctx_set_tuning", C.c_int, [vp, C.c_int, C.POINTER(C.c_uint64), i32p]),
+    ("pq_ctx_tuning_size", C.c_int, [vp, C.POINTER(C.c_int)]),
+    ("pq_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
+    ("pq_pair_tuning", C.c_int, [vp, C.c_int, C.c_int, i32p, i64p, C.POINTER(C.c_uint64), C.c_int, i32p,
+                                 C.POINTER(C.c_int)]),
 ]
 
 # exported by the library but optional for older builds

@@ -72,6 +72,7 @@ class GB300Backend:
             raise L.PQError(rc, f"pq_ctx_create(device={device}, precision={precision}) failed")
         self.ctx = h
         self.precision = precision
+        self.device = device
         if small_elems is not None:
             self._check(self.lib.pq_ctx_set_small_elems(self.ctx, int(small_elems)), "set_small_elems")
         self.metrics = Metrics()
@@ -96,6 +97,12 @@ class GB300Backend:
 
     def _check(self, rc, what):
         L.check(rc, self.ctx, what)
+
+    def tuning_size(self) -> int:
+        """Entries of the context's autotuned table (``autotune``)."""
+        n = C.c_int()
+        self._check(self.lib.pq_ctx_tuning_size(self.ctx, C.byref(n)), "tuning_size")
+        return n.value
 
     def id_of(self, label) -> int:
         key = str(label)

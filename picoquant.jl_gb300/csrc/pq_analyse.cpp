@@ -59,7 +59,8 @@ static void merge_modes(std::vector<Mode>& v) {
 
 bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
                   const std::vector<int>& lb, const std::vector<int64_t>& db,
-                  const std::vector<int>& lc, int precision, PairPlan& out, std::string& err) {
+                  const std::vector<int>& lc, int precision, PairPlan& out, std::string& err,
+                  const TuningTable* tune) {
   if (la.size() != da.size() || lb.size() != db.size()) {
     err = "label/dim count mismatch";
     return false;
@@ -250,6 +251,17 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
     out.kclass = KC_GEMM;
   else
     out.kclass = KC_GENERIC;
+  out.k_both = k_both;
+  out.gemm_shape = gemm_shape;
+  if (tune && !tune->empty() && k_both) {
+    auto it = tune->find(tuning_key(precision, G));
+    if (it != tune->end() && choice_eligible(precision, out, it->second)) {
+      out.kclass = (KernelClass)it->second.kclass;
+      G.tile_n = it->second.kclass == KC_TC ? it->second.tile_n : 0;
+      G.orient = it->second.kclass == KC_TC ? it->second.orient : 0;
+      out.tuned = true;
+    }
+  }
   return true;
 }
 

@@ -407,7 +407,7 @@ int pq_contract_tensors(pq_ctx* c, int64_t a, const int32_t* a_labels, int a_ran
   std::vector<int> lc = symdiff_labels(la, lb);
   PairPlan pp;
   std::string err;
-  if (!analyse_pair(la, A.dims, lb, B.dims, lc, ctx->precision, pp, err))
+  if (!analyse_pair(la, A.dims, lb, B.dims, lc, ctx->precision, pp, err, &ctx->tuning))
     return fail(ctx, PQ_ERR_INVALID, "contract_tensors: " + err);
   Tensor C;
   int st = alloc_tensor(ctx, pp.c_dims, storage_dtype(ctx, pp.csize), C);

@@ -45,6 +45,10 @@ struct GemmDesc {
   int64_t ndim[kMaxModes], nsb[kMaxModes], nsc[kMaxModes];
   int64_t kdim[kMaxModes], ksa[kMaxModes], ksb[kMaxModes];
   int64_t zdim[kMaxModes], zsa[kMaxModes], zsb[kMaxModes], zsc[kMaxModes];
+  // Autotuned launch shape of the exact-accumulation tensor-core class:
+  // tile_n = columns per tile (16/32/64/128; 0 = the default rule), orient =
+  // 1 to run as given, 2 to run as C = B x A (0 = the default rule).
+  int tile_n, orient;
 };
 
 enum KernelClass : int { KC_GENERIC = 0, KC_GEMM = 1, KC_TC = 2, KC_COPY = 3, KC_SKINNY = 4 };
@@ -69,14 +73,34 @@ struct PairPlan {
   GemmDesc m;
   int64_t run_a = 1, run_b = 1;   // extent of the unit-stride run of A / B that
                                    // is read contiguously (coalescing feature)
+  bool k_both = false;      // every contracted mode is in both operands
+  bool gemm_shape = false;  // large enough for the tiled GEMM classes
+  bool tuned = false;       // the class came from the tuning table
 };
+
+// Autotuning (pq_tune.cpp).  A tuning class is the pair's precision mode, the
+// ceil-log2 of its M, N, K and batch extents and whether the unit-stride mode
+// of A / of B is contracted; a choice is a kernel class plus, for the
+// exact-accumulation tensor-core class, a tile width and an orientation.
+struct TuneChoice {
+  int kclass;
+  int tile_n;
+  int orient;
+};
+using TuningTable = std::unordered_map<uint64_t, TuneChoice>;
+uint64_t tuning_key(int precision, const GemmDesc& d);
+// Every choice the kernels can run for this analysed pair (the default first).
+std::vector<TuneChoice> tuning_candidates(int precision, const PairPlan& p);
+bool choice_eligible(int precision, const PairPlan& p, const TuneChoice& c);
 
 // Analyse C = A x B given labels (A/B storage order) and the result labels
 // (storage order).  Labels of A or B absent from C are summed.  Returns
-// false with `err` set on inconsistent input.
+// false with `err` set on inconsistent input.  With a tuning table, a pair
+// whose class is in the table runs the table's choice when eligible.
 bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
                   const std::vector<int>& lb, const std::vector<int64_t>& db,
-                  const std::vector<int>& lc, int precision, PairPlan& out, std::string& err);
+                  const std::vector<int>& lc, int precision, PairPlan& out, std::string& err,
+                  const TuningTable* tune = nullptr);
 
 // Result labels in the reference's order: A's labels not in B (A order),
 // then B's labels not in A (B order).
@@ -114,6 +138,9 @@ struct Ctx {
   // complex128 (gates, per-qubit tensors: cheap, and their rounding would
   // dominate the error) and larger ones as complex64.
   int64_t small_elems = int64_t(1) << 16;
+  // Autotuned choices per tuning class (pq_ctx_set_tuning), consulted when
+  // pairs are analysed (contractions, plans, measurements).
+  TuningTable tuning;
 };
 
 inline size_t elem_bytes(int dt) { return dt == PQ_C128 ? 16 : 8; }

@@ -34,7 +34,7 @@ int pq_measure_pairs(pq_ctx* c, int n_pairs, const int32_t* a_ranks, const int32
     std::vector<int64_t> db(dims + pos, dims + pos + b_ranks[p]);
     pos += b_ranks[p];
     std::string err;
-    if (!analyse_pair(la, da, lb, db, symdiff_labels(la, lb), ctx->precision, plans[p], err))
+    if (!analyse_pair(la, da, lb, db, symdiff_labels(la, lb), ctx->precision, plans[p], err, &ctx->tuning))
       return fail(ctx, PQ_ERR_INVALID, "measure_pairs: pair " + std::to_string(p) + ": " + err);
     const PairPlan& q = plans[p];
     ta[p] = storage_dtype(ctx, q.asize);

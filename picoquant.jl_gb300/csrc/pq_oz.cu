@@ -715,6 +715,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 int oz_tile_n(int64_t n) { return n <= 16 ? 16 : (n <= 32 ? 32 : (n <= 64 ? 64 : 128)); }
+// Tile width of an oriented pair: the autotuner's choice when it set one,
+// else the narrowest tile that covers N (at most 128).
+int oz_tile_of(const GemmDesc& d) {
+  return (d.tile_n == 16 || d.tile_n == 32 || d.tile_n == 64 || d.tile_n == 128) ? d.tile_n : oz_tile_n(d.N);
+}
 
 struct OzLayout {
   int tn;
@@ -724,7 +729,7 @@ struct OzLayout {
 
 OzLayout layout(const GemmDesc& d, int nsl) {
   OzLayout L;
-  L.tn = oz_tile_n(d.N);
+  L.tn = oz_tile_of(d);
   L.mt = ceil_div(d.M, kRows);
   L.nt = ceil_div(d.N, L.tn);
   L.kt = ceil_div(d.K, TK);
@@ -760,7 +765,13 @@ GemmDesc swapped(const GemmDesc& d) {
   }
   return s;
 }
-bool needs_swap(const GemmDesc& d) { return d.M < 64 && d.N > d.M; }
+// Orientation: the autotuner's choice (orient 1 = as given, 2 = swapped) when
+// it set one, else swap when A is the narrow side.
+bool needs_swap(const GemmDesc& d) {
+  if (d.orient == 1) return false;
+  if (d.orient == 2) return true;
+  return d.M < 64 && d.N > d.M;
+}
 
 template <typename T, int ROWS, int NSL>
 void prep_b(const void* X, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
@@ -815,7 +826,7 @@ bool eligible_oriented(const GemmDesc& d) {
   // a 16-column gate tensor over K = 16): memory-bound work whose per-tile
   // costs here exceed a plain FP32 pass, and whose FP32 sums have <= 32 terms
   if (d.N * d.K < 512) return false;
-  if (d.Z > 65535 || ceil_div(d.N, oz_tile_n(d.N)) > 65535) return false;  // grid y / z of the B passes
+  if (d.Z > 65535 || ceil_div(d.N, oz_tile_of(d)) > 65535) return false;  // grid y / z of the B passes
   return layout(d, 5).total <= (size_t(24) << 30);
 }
 

@@ -359,7 +359,7 @@ bool compile(const Ctx* ctx, const std::vector<std::vector<int>>& leaf_labels,
     s.y = y;
     s.batched = batched[x] || batched[y];
     batched[r] = s.batched;
-    if (!analyse_pair(cp.labels[x], cp.dims[x], cp.labels[y], cp.dims[y], lr, precision, s.pp, err)) {
+    if (!analyse_pair(cp.labels[x], cp.dims[x], cp.labels[y], cp.dims[y], lr, precision, s.pp, err, &ctx->tuning)) {
       err = "step " + std::to_string(i) + ": " + err;
       return false;
     }

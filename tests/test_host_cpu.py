@@ -499,3 +499,33 @@ def test_oracle_amplitude_along_plan_record(pq, O):
     rec["leaves"] = nodes[1:] + nodes[:1]
     with pytest.raises(RuntimeError):
         bench.oracle_network(O, rec)
+
+
+def test_autotune_plan_pairs_and_names(pq):
+    """The tuner's view of a plan: each step's operand labels and extents
+    under the executor's label rule, steps keeping a shared label skipped;
+    and readable choice names."""
+    from pqgb300 import autotune as AT
+
+    class Plan:
+        ranks = [2, 2, 2, 1]
+        flat = [0, 1, 1, 2, 2, 3, 3]
+        out_labels = [0]
+        steps = [0, 1, 4, 2, 5, 3]
+        dims = [4, 8, 3, 5]
+
+    pairs = AT.plan_pairs(Plan)
+    assert pairs[0] == ([0, 1], [4, 8], [1, 2], [8, 3])
+    assert pairs[1] == ([0, 2], [4, 3], [2, 3], [3, 5])
+    assert pairs[2] == ([0, 3], [4, 5], [3], [5])
+
+    class Hyper:  # label 1 is carried by three leaves: the first step keeps it
+        ranks = [2, 1, 1]
+        flat = [0, 1, 1, 1]
+        out_labels = [0]
+        steps = [0, 1, 3, 2]
+        dims = [2, 3]
+
+    assert AT.plan_pairs(Hyper) == [([0, 1], [2, 3], [1], [3])]
+    assert AT.choice_name((2, 64, 2)) == "tcgen05/tn64/swapped" and AT.choice_name((4, 0, 0)) == "skinny"
+    assert len(AT.source_hash()) == 16
