@@ -517,15 +517,39 @@ def run_learned(args, rows=7, cols=7, depth=14):
         t1 = time.perf_counter()
         amplitude(plan, sliced)
         ts.append(time.perf_counter() - t1)
-    # the flop-count planner's choice, same precision
+    # the flop-count planner's choice, same precision, timed the same way
+    # (warm, then --steps runs), interleaved with the learned plan's
     pf = pq.NetworkPlan(net, steps=best_flop["steps"], out_edges=[])
     sf = pf.choose_slices(max_sliced=10, log2_target=target)
-    t1 = time.perf_counter()
-    amp_f = amplitude(pf, sf)
-    t_flop = time.perf_counter() - t1
+    amp_f = None
+    for _ in range(max(1, args.warmup - 1)):
+        amp_f = amplitude(pf, sf)
+    be.sync()
+    tf, tl = [], []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        amp_f = amplitude(pf, sf)
+        tf.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        amplitude(plan, sliced)
+        tl.append(time.perf_counter() - t1)
+    t_flop = float(np.median(tf)) if tf else None
+    t_learned = float(np.median(tl)) if tl else None
     pf.close()
     plan.close()
     be.close()
+    # the FP64 oracle's contraction of the same amplitude along the learned plan
+    oracle = None
+    if args.oracle == "full":
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import tn_oracle as O  # the checker
+
+        nodes = list(net.nodes)
+        rec = {"rows": rows, "cols": cols, "depth": depth, "circuit_seed": 2026, "bitstring": bits,
+               "leaves": nodes, "leaf_indices": [list(net.nodes[x].indices) for x in nodes], "steps": chosen["steps"]}
+        amp_o, t_o = oracle_amplitude(O, rec)
+        oracle = {"amplitude": [amp_o.real, amp_o.imag], "seconds": t_o, "threads": host_threads(),
+                  "rel_err": abs(amp - amp_o) / abs(amp_o)}
     # the plain complex-FP64 path on the flop-count plan
     be64 = pq.GB300Backend(pq.PREC_C128)
     net64 = network(be64)
@@ -545,7 +569,11 @@ def run_learned(args, rows=7, cols=7, depth=14):
             "learned_plan": {"name": chosen["name"], "log2_cmacs": float(np.log2(chosen["cmacs"])),
                              "pred_us": chosen["pred_us"]},
             "flop_plan": {"name": best_flop["name"], "log2_cmacs": float(np.log2(best_flop["cmacs"])),
-                          "seconds": t_flop},
+                          "seconds": t_flop, "sliced_bonds": len(sf)},
+            "learned_plan_seconds": t_learned,
+            "learned_gain_over_flop_plan": (t_flop / t_learned) if (t_flop and t_learned) else None,
+            "timing": "median of --steps warm runs per plan, interleaved (host clock, result read back)",
+            "oracle": oracle, "rel_err_vs_oracle": oracle["rel_err"] if oracle else None,
             "candidates": len(cands), "candidates_within_flop_judge": len(ranked),
             "model_ranking_top5": [(c["name"], c["pred_us"], len(c.get("sliced", []))) for c in ranked[:5]],
             "sliced_bonds": len(sliced), "slice_target_log2": target,
@@ -869,6 +897,9 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
     roof = None
     cpu = None
     ms_step = 1e3 * t_total / args.steps
+    sp = C.c_void_p()
+    be.lib.pq_ctx_stream(be.ctx, C.byref(sp))
+    ext = torch.cuda.ExternalStream(sp.value)
     if args.workload == "grid6x6_d16_sliced":
         sliced = w["sliced"]
         ms, batched, feats = plan.profile_sliced(sliced, batch=args.batch)
@@ -887,6 +918,36 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
                          "sliced_bonds": len(sliced), "planning_s": w["t_plan"], "plan_sha": plan_sha(rec["steps"]),
                          "same_plan_as_reference_arm": bool(ref_rec is not None and ref_rec["steps"] == rec["steps"]
                                                             and ref_rec["leaves"] == rec["leaves"])}
+        # the flop-count planner's own pick (the method without the learned
+        # model) on the same backend and tuned table, timed like the headline
+        fsteps, fcm, fmx, fname = pq.planning.best_flop_plan(w["net"], out_edges=[], candidates=("sweep",),
+                                                              sweep_random=SWEEP_RANDOM)
+        flop = {"planner": "flop:" + fname, "log2_cmacs": float(np.log2(fcm)),
+                "same_as_learned": list(fsteps) == list(plan.steps)}
+        if not flop["same_as_learned"]:
+            pf = pq.NetworkPlan(w["net"], steps=fsteps, out_edges=[])
+            sf = pf.choose_slices(max_sliced=len(sliced), log2_target=args.slice_target)
+            bf = pf.auto_batch(sf)
+            for _ in range(2):
+                pf.run_sliced(sf, batch=bf)
+
+            def timed(fn):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                fn()
+                e1.record(ext)
+                e1.synchronize()
+                return e0.elapsed_time(e1)
+
+            tfl, tle = [], []
+            for _ in range(max(3, args.fp64_steps)):  # interleaved, no L2 flush for either
+                tfl.append(timed(lambda: pf.run_sliced(sf, batch=bf)))
+                tle.append(timed(lambda: plan.run_sliced(sliced, batch=args.batch)))
+            pf.close()
+            flop["ms_per_amplitude"] = float(np.median(tfl))
+            flop["learned_ms_per_amplitude"] = float(np.median(tle))
+            extra["learned_gain_over_flop_plan"] = flop["ms_per_amplitude"] / flop["learned_ms_per_amplitude"]
+        extra["flop_plan"] = flop
         # the plain complex-FP64 CUDA path on the same amplitude along the same
         # plan, timed warm with CUDA events on its context's stream
         a64 = None

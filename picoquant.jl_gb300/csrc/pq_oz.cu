@@ -376,10 +376,20 @@ __device__ __forceinline__ float two_sum(float a, float b, float& e) {
   e = (a - (s - bb)) + (b - bb);
   return s;
 }
-__device__ __forceinline__ float combine(float l0, float l1, float l2, int ex, float) {
+// (l0 + l1 + l2) rounded once (before scaling): l0 + l1 by an error-free
+// two-sum, the small l2 added to its error term.
+__device__ __forceinline__ float level_sum(float l0, float l1, float l2) {
   float e;
   const float s = two_sum(l0, l1, e);
-  return ldexpf(s + (e + l2), ex);
+  return s + (e + l2);
+}
+// x 2^ex with one rounding, the same value as ldexpf(x, ex): a multiply by an
+// exact power of two when 2^ex is a normal float.
+__device__ __forceinline__ float scale_pow2(float x, int ex) {
+  return (ex >= -126 && ex <= 127) ? x * __int_as_float((ex + 127) << 23) : ldexpf(x, ex);
+}
+__device__ __forceinline__ float combine(float l0, float l1, float l2, int ex, float) {
+  return scale_pow2(level_sum(l0, l1, l2), ex);
 }
 __device__ __forceinline__ double combine(float l0, float l1, float l2, int ex, double) {
   return ldexp(((double)l0 + (double)l1) + (double)l2, ex);
@@ -629,6 +639,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     using R = typename std::conditional<std::is_same<TC, double2>::value, double, float>::type;
     R* Cr = reinterpret_cast<R*>(C);
     constexpr int PW = CW >= 16 ? 16 : 8;   // columns per TMEM load
+    // One accumulator set and complex64 results: the combined levels are
+    // parked in the unused fourth TMEM block so that the accumulators are
+    // released before the scaling and the scattered stores.
+    constexpr bool kStash = kSets == 1 && std::is_same<TC, float2>::value && 4 * TN <= (int)kTmemCols &&
+                            CW % 16 == 0;
     constexpr int NU = (CW + 31) / 32;       // columns of the warp's range per lane
     // per-tile offsets and scales, loaded one tile ahead: the row's from
     // this lane, the warp's columns spread over the lanes
@@ -671,6 +686,49 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       fence_after();
+      if constexpr (kStash) {
+        // Phase 1 (holds the accumulators): the three levels of each element
+        // summed into one float, parked in the spare TMEM block (columns
+        // 3 TN .. 4 TN, the same lanes); then the accumulators are released.
+#pragma unroll
+        for (int piece = 0; piece < CW / 16; ++piece) {
+          __syncwarp();
+          const uint32_t col = (uint32_t)(h * CW + piece * 16);
+          float l0[16], l1[16], l2[16];
+          tmem_ld16(lane_base + col + 0 * TN, l0);
+          tmem_ld16(lane_base + col + 1 * TN, l1);
+          tmem_ld16(lane_base + col + 2 * TN, l2);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; ++j) l0[j] = level_sum(l0[j], l1[j], l2[j]);
+          tmem_st16(lane_base + 3 * TN + col, l0);
+        }
+        tmem_wait_st();
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acce[b]);
+        // Phase 2 (overlaps the next tile's MMAs): scale by 2^(ea + eb) and
+        // scatter through the result index map.
+#pragma unroll
+        for (int piece = 0; piece < CW / 16; ++piece) {
+          __syncwarp();
+          float v[16];
+          tmem_ld16(lane_base + 3 * TN + (uint32_t)(h * CW + piece * 16), v);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int cc = piece * 16 + j;
+            const int ebj = __shfl_sync(0xffffffffu, M.ebl[cc / 32], cc % 32);
+            const long long cnj = __shfl_sync(0xffffffffu, M.cnl[cc / 32], cc % 32);
+            if (mrow && c0 + cc < d.N) {
+              const int ex = exa + ebj;
+              const R val = (exa == kExpZero || ex < -2 * 1100) ? (R)0 : (R)scale_pow2(v[j], ex);
+              Cr[2 * (base + cnj) + part] = val;
+            }
+          }
+        }
+        continue;
+      }
 #pragma unroll
       for (int piece = 0; piece < CW / PW; ++piece) {
         __syncwarp();  // the TMEM loads are warp-collective

@@ -156,3 +156,37 @@ def test_trained_weights_file_loads(pq, be):
     X = CM.model_inputs(np.array([[20, 16, 20, 8, 3, 4, 1, 1e7]], dtype=np.float64))
     assert np.isfinite(m.predict(X)).all()
     m.close()
+
+
+def test_learned_plan_gains_over_flop_plan(pq, O):
+    """What the trained network gains over the method without it: on the
+    4x5 depth-12 open-output network the cost model ranks a Boltzmann-greedy
+    draw first, while the flop-count planner (the judge and fallback) picks
+    the reference's full-wavefunction order with fewer multiply-adds.  Both
+    plans run as CUDA graphs, timed interleaved; the learned pick must not be
+    slower (it ran 1.14x faster when the model was trained), and both give
+    the oracle's state."""
+    from pqgb300 import costmodel as CM
+    from pqgb300.train_costmodel import time_plan
+
+    be = pq.GB300Backend(pq.PREC_OZAKI)
+    gates = pq.random_grid_gates(4, 5, 12, seed=2024)
+    net = pq.build_network(20, gates, backend=be)
+    pq.add_input(net, "0" * 20)
+    model = CM.CostModel.load(be)
+    chosen, best_flop, cands = CM.learned_plan(net, model, out_edges=None, n_random=16)
+    model.close()
+    assert chosen["name"] != best_flop["name"] and chosen["cmacs"] > best_flop["cmacs"]
+    oe = pq.open_output_edges(net)
+    tl, tf = [], []
+    for _ in range(3):
+        t, r_l = time_plan(pq, net, chosen["steps"], oe, reps=10)
+        tl.append(t)
+        t, r_f = time_plan(pq, net, best_flop["steps"], oe, reps=10)
+        tf.append(t)
+    assert min(tl) <= min(tf), (chosen["name"], tl, best_flop["name"], tf)
+    sv = O.statevector(20, O.random_grid_gates(4, 5, 12, seed=2024))
+    for r in (r_l, r_f):
+        v = np.asarray(r).reshape(-1, order="F")
+        assert np.max(np.abs(v - sv)) <= 1e-6 * np.max(np.abs(sv))
+    be.close()

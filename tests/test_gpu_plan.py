@@ -342,3 +342,41 @@ def test_small_step_groups_mixed_extents(pq, O, prec):
     T = [x[0] for x in leaves]
     ref = np.einsum("ak,km,mb,cl,ln,nb,dp,pq,qb->acd", *T)
     assert rel(got, ref) < TOL[prec]
+
+
+def test_grid7x7_d14_amplitude_vs_oracle(pq, O):
+    """A single amplitude of the 7x7 depth-14 random circuit (49 qubits, the
+    learned-planning workload's size) on the exact-accumulation path, along
+    the flop-count planner's sweep plan (2^36.5 complex multiply-adds,
+    intermediates up to 2^26 elements), unsliced and with the heavy subtree
+    sliced (ten bonds chosen for a 2^22-element target: per-slice
+    intermediates of at most 2^24 elements, part of the work repeated per
+    slice), against the FP64 oracle's contraction of the same network
+    along the same plan: relative error <= 1e-6 both ways."""
+    import bench
+
+    rows, cols, depth = 7, 7, 14
+    n = rows * cols
+    gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
+    bits = pq.random_bitstrings(n, 1, seed=2027)[0]
+    be = pq.GB300Backend(pq.PREC_OZAKI)
+    net = pq.build_network(n, gates, decompose=True, backend=be)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, bits)
+    steps, cm, mx, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    nodes = list(net.nodes)
+    rec = {"rows": rows, "cols": cols, "depth": depth, "circuit_seed": 2026, "bitstring": bits, "leaves": nodes,
+           "leaf_indices": [list(net.nodes[x].indices) for x in nodes], "steps": steps}
+    ref, _ = bench.oracle_amplitude(O, rec)
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    plan.execute()
+    amp = complex(np.asarray(plan.result()).reshape(-1)[0])
+    assert abs(amp - ref) <= 1e-6 * abs(ref), (amp, ref)
+    sl = plan.choose_slices(max_sliced=10, log2_target=22.0)
+    assert len(sl) >= 4
+    sizes = plan.sliced_sizes(sl)
+    assert max(x for x, _ in sizes) <= np.log2(mx) - 2
+    amp_s = plan.run_sliced(sl, batch=plan.auto_batch(sl))
+    assert abs(amp_s - ref) <= 1e-6 * abs(ref), (amp_s, ref, sizes)
+    plan.close()
+    be.close()
