@@ -110,17 +110,18 @@ SWEEP_RANDOM = 64
 
 
 def build_sliced(pq, precision, rows=6, cols=6, depth=16, n_sliced=10, seed=2026, rank=0, target=28.0,
-                 planner="learned", steps=None, tuning="off"):
+                 planner="learned", steps=None, tuning="off", storage="c64"):
     """The sliced single-amplitude workload on a new backend of ``precision``:
     network, plan (``steps`` if given, else the named planner's choice) and
     the sliced bonds chosen for a 2^target-element intermediate limit.
     ``tuning="cache"``: the autotuner's table for this GPU is loaded (the
     plan's classes it lacks tuned and the cache written back) and the plan
-    compiled under it."""
+    compiled under it.  ``storage="c128"`` stores every tensor as complex128
+    (the mixed modes otherwise store large tensors as complex64)."""
     n = rows * cols
     gates = pq.random_grid_gates(rows, cols, depth, seed=seed)
     bits = pq.random_bitstrings(n, 1, seed=seed + 1 + rank)[0]
-    be = pq.GB300Backend(precision)
+    be = pq.GB300Backend(precision, small_elems=(1 << 62) if storage == "c128" else None)
     net = pq.build_network(n, gates, decompose=True, backend=be)
     pq.add_input(net, "0" * n)
     pq.add_output(net, bits)
@@ -243,13 +244,18 @@ def main():
     ap.add_argument("--circuits", type=int, default=512, help="circuits of the uneven512 workload")
     ap.add_argument("--amplitudes", type=int, default=8, help="amplitudes of the grid6x6_d16_accuracy workload")
     ap.add_argument("--check", type=int, default=8, help="uneven512 circuits also run in complex128 for the error")
+    ap.add_argument("--sv-budget-gb", type=float, default=64.0,
+                    help="uneven512: state bytes resident at once in the grouped state-vector batch")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
     ap.add_argument("--pair-order", default="mk", choices=["mk", "km"],
                     help="memory order of the pair's A: contiguous along M (mk) or along K (km)")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
     ap.add_argument("--cols", type=int, default=6)
     ap.add_argument("--depth", type=int, default=16)
-    ap.add_argument("--precision", default="auto", choices=["auto", "c64", "3xtf32", "6xtf32", "ozaki", "3xbf16", "c128"])
+    ap.add_argument("--precision", default="auto",
+                    choices=["auto", "c64", "3xtf32", "6xtf32", "ozaki", "ozaki4", "3xbf16", "c128"])
+    ap.add_argument("--storage", default="c64", choices=["c64", "c128"],
+                    help="storage of large tensors in the mixed-precision modes (c128: every tensor complex128)")
     ap.add_argument("--batch", type=int, default=0, help="slices per launch (0: sized from memory)")
     ap.add_argument("--ref-budget", type=float, default=150.0,
                     help="seconds of whole-amplitude CPU steps the reference arm times (at least one step)")
@@ -294,11 +300,17 @@ def run_accuracy(args):
     pq = g.load_package()
     prec_name = args.precision if args.precision != "auto" else "ozaki"
     prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
-            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
-    errs, scaled = [], []
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128, "ozaki4": pq.PREC_OZAKI4}[prec_name]
+    errs, scaled, secs = [], [], []
     for r in range(args.amplitudes):
-        w = build_sliced(pq, prec, args.rows, args.cols, args.depth, rank=r, target=args.slice_target)
-        a = w["plan"].run_sliced(w["sliced"], batch=w["plan"].auto_batch(w["sliced"]))
+        w = build_sliced(pq, prec, args.rows, args.cols, args.depth, rank=r, target=args.slice_target,
+                         storage=args.storage)
+        bat = w["plan"].auto_batch(w["sliced"])
+        for _ in range(2):  # the second identical run records the CUDA graph
+            a = w["plan"].run_sliced(w["sliced"], batch=bat)
+        t0 = time.perf_counter()
+        a = w["plan"].run_sliced(w["sliced"], batch=bat)
+        secs.append(time.perf_counter() - t0)
         w["plan"].close()
         w["be"].close()
         w64 = build_sliced(pq, pq.PREC_C128, args.rows, args.cols, args.depth, rank=r, target=args.slice_target,
@@ -311,7 +323,9 @@ def run_accuracy(args):
     line = {"workload": f"grid{args.rows}x{args.cols}_depth{args.depth}_sliced_accuracy", "precision": prec_name,
             "metric": "relative amplitude error vs the plain complex-FP64 GPU path", "amplitudes": len(errs),
             "rel_errors": errs, "rms": float(np.sqrt(np.mean(np.square(errs)))), "max": float(np.max(errs)),
-            "max_err_over_2^-n/2": float(np.max(scaled)), "target": 1e-6,
+            "max_err_over_2^-n/2": float(np.max(scaled)), "target": 1e-6, "storage": args.storage,
+            "ms_per_amplitude": [1e3 * x for x in secs],
+            "timing": "third run of each amplitude (graph replay, host clock, result read back)",
             "plans": "learned plan (mixed) vs flop-count plan (FP64)", "data": "synthetic (seeded random circuit)"}
     print(json.dumps(line))
     return 0
@@ -346,20 +360,26 @@ def run_uneven(args):
     (qubits uniform in 12..30, grid factorised from the count, depth uniform
     in 8..24), 64 random-bitstring amplitudes each.  Per circuit the cheaper
     of two strategies by a roofline estimate: the state vector (gates fused
-    into blocks of at most four qubits, one pass over the state per block, the
-    64 amplitudes gathered) or the qubit-sweep tensor-network order with the 64 output
-    bitstrings as one batch index.  Every plan is compiled, captured as a CUDA
-    graph and launched from it; a step contracts all circuits.  The first
-    ``--check`` circuits are also run in complex128 for the error."""
+    into blocks of at most four qubits) or the qubit-sweep tensor-network
+    order with the 64 output bitstrings as one batch index.  All state-vector
+    circuits run as one grouped batch (``StateVectorBatch``: circuits packed
+    by size into chunks under a memory budget, launch s applying every
+    circuit's s-th block, the whole batch one CUDA graph); each sweep circuit
+    is a compiled plan captured as a CUDA graph.  Compilation and capture
+    happen once (reported); a step replays everything and reads all
+    amplitudes back.  The first ``--check`` circuits are also run in
+    complex128, and a seeded sample of up to 16 circuits of at most 20 qubits
+    is checked against the FP64 oracle's state vector."""
     import __graft_entry__ as g
 
     pq = g.load_package()
     from pqgb300 import circuits as CI
     from pqgb300 import planning as PL
+    from pqgb300.svbatch import StateVectorBatch
 
     prec_name = args.precision if args.precision != "auto" else "ozaki"
     prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
-            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128, "ozaki4": pq.PREC_OZAKI4}[prec_name]
     rng = np.random.default_rng(2026)
     specs = [(int(rng.integers(12, 31)), int(rng.integers(8, 25))) for _ in range(args.circuits)]
     t0 = time.perf_counter()
@@ -378,76 +398,132 @@ def run_uneven(args):
         sw, cm, mx = PL.sweep_steps(hn, nodes, [label_of[AMP_INDEX]], label_of, ranks, flat, dims)
         t_sw = cm * 8 / 40e12 + len(sw) // 2 * 4e-6 if mx * 8 < 2 ** 34 else float("inf")
         if t_sv <= t_sw:
-            plans.append(dict(kind="statevector", n=n, d=d, gates=fused, bits=bits, decompose=False, steps=None))
+            plans.append(dict(kind="statevector", n=n, d=d, r=r, c=c, i=i, fused=fused, gates=gates, bits=bits))
         else:
-            plans.append(dict(kind="sweep", n=n, d=d, gates=gates, bits=bits, decompose=True, steps=sw))
+            plans.append(dict(kind="sweep", n=n, d=d, r=r, c=c, i=i, gates=gates, bits=bits, steps=sw))
     t_plan = time.perf_counter() - t0
+    sv_ids = [k for k, p in enumerate(plans) if p["kind"] == "statevector"]
+    sw_ids = [k for k, p in enumerate(plans) if p["kind"] == "sweep"]
 
-    def networks(be, count=None):
-        # all circuits share one backend: node labels (the backend's tensor
-        # names) start at a distinct offset per circuit
+    def sweep_network(be, ci, p):
         from pqgb300 import network as NW
 
-        nets = []
-        for ci, p in enumerate(plans[:count]):
-            net = NW.TensorNetworkCircuit(p["n"], be)
-            net.counters["node"] = ci * 10_000_000
-            for U, qs in p["gates"]:
-                NW.add_gate(net, CI.operator_to_tensor(U), qs, decompose=p["decompose"])
-            pq.add_input(net, "0" * p["n"])
-            if p["kind"] == "sweep":
-                batched_outputs(pq, net, p["bits"])
-                nets.append((net, p["steps"], [AMP_INDEX]))
-            else:
-                nets.append((net, PL.statevector_steps(net), None))
-        return nets
+        net = NW.TensorNetworkCircuit(p["n"], be)
+        net.counters["node"] = ci * 10_000_000  # distinct tensor names per circuit on one backend
+        for U, qs in p["gates"]:
+            NW.add_gate(net, CI.operator_to_tensor(U), qs, decompose=True)
+        pq.add_input(net, "0" * p["n"])
+        batched_outputs(pq, net, p["bits"])
+        return net
 
-    def run_all(nets, count=None):
-        out = []
-        for (net, steps, oe), p in list(zip(nets, plans))[:count]:
-            plan = pq.NetworkPlan(net, steps=steps, out_edges=oe)
-            res = plan.capture()
-            if p["kind"] == "sweep":
-                a = np.asarray(net.backend.load_tensor_data(res)).reshape(-1)
-            else:
-                a = net.backend.gather(res, PL.bitstrings_to_index(p["bits"]))
-                net.backend.delete_tensor(res)
-            plan.close()
-            out.append(a)
-        return out
+    def compile_all(be, ids_sv, ids_sw, budget):
+        sb = StateVectorBatch(be, [(plans[k]["n"], plans[k]["fused"], plans[k]["bits"]) for k in ids_sv],
+                              state_budget_bytes=budget) if ids_sv else None
+        sweeps = []
+        for k in ids_sw:
+            net = sweep_network(be, k, plans[k])
+            plan = pq.NetworkPlan(net, steps=plans[k]["steps"], out_edges=[AMP_INDEX])
+            out = plan.capture()
+            sweeps.append((k, plan, out))
+        return (sb, list(ids_sv)), sweeps
 
+    def run_all(be, sbk, sweeps):
+        amps = {}
+        sb, keys = sbk
+        if sb is not None:
+            for k, a in zip(keys, sb.execute()):
+                amps[k] = a
+        for k, plan, out in sweeps:
+            plan.execute(out)
+            amps[k] = np.asarray(be.load_tensor_data(out)).reshape(-1)
+        return amps
+
+    budget = int(args.sv_budget_gb * (1 << 30))
     be = pq.GB300Backend(prec)
     t1 = time.perf_counter()
-    nets = networks(be)
-    t_build = time.perf_counter() - t1
-    for _ in range(min(1, args.warmup)):
-        run_all(nets)
+    sbk, sweeps = compile_all(be, sv_ids, sw_ids, budget)
+    sb = sbk[0]
+    t_compile = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    amps = run_all(be, sbk, sweeps)  # first pass records the state-vector graph
+    t_first = time.perf_counter() - t1
     be.sync()
-    ts, amps = [], None
+    launches0 = be.launch_count()
+    ts = []
     for _ in range(max(1, args.steps)):
         t1 = time.perf_counter()
-        amps = run_all(nets)
+        amps = run_all(be, sbk, sweeps)
         be.sync()
         ts.append(time.perf_counter() - t1)
+    launches = (be.launch_count() - launches0) / max(1, args.steps)
+    sb_info = sb.info() if sb is not None else {}
+    if sb is not None:
+        sb.close()
+    for _, plan, _ in sweeps:
+        plan.close()
     be.close()
-    # complex128 on the first circuits, same strategies
+    # complex128 on the first --check circuits, same strategies
     k = min(args.check, len(plans))
+    chk = list(range(k))
+    chk_sv = [x for x in chk if plans[x]["kind"] == "statevector"]
+    chk_sw = [x for x in chk if plans[x]["kind"] == "sweep"]
+    # (the state-vector circuits as per-circuit complex128 plans: the grouped
+    # batch itself always keeps complex64 states)
     be64 = pq.GB300Backend(pq.PREC_C128)
-    ref = run_all(networks(be64, k), k) if k else []
+    _, sweeps64 = compile_all(be64, [], chk_sw, budget)
+    ref64 = run_all(be64, (None, []), sweeps64)
+    for _, plan, _ in sweeps64:
+        plan.close()
+    for x in chk_sv:
+        from pqgb300 import network as NW
+
+        p = plans[x]
+        net = NW.TensorNetworkCircuit(p["n"], be64)
+        net.counters["node"] = (len(plans) + x) * 10_000_000
+        for U, qs in p["fused"]:
+            NW.add_gate(net, CI.operator_to_tensor(U), qs, decompose=False)
+        pq.add_input(net, "0" * p["n"])
+        plan = pq.NetworkPlan(net, steps=PL.statevector_steps(net))
+        res = plan.capture()
+        ref64[x] = be64.gather(res, PL.bitstrings_to_index(p["bits"]))
+        be64.delete_tensor(res)
+        plan.close()
     be64.close()
-    errs = [float(np.max(np.abs(a - b)) / np.sqrt(np.mean(np.abs(b) ** 2))) for a, b in zip(amps[:k], ref)]
+    errs = [float(np.max(np.abs(amps[x] - ref64[x])) / np.sqrt(np.mean(np.abs(ref64[x]) ** 2))) for x in chk]
+    # the FP64 oracle's state vector of the original gates, on a seeded sample
+    oracle_errs = []
+    if args.oracle == "full":
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import tn_oracle as O  # the checker
+
+        small = [x for x in range(len(plans)) if plans[x]["n"] <= 20]
+        sample = sorted(np.random.default_rng(7).choice(small, size=min(16, len(small)), replace=False).tolist())
+        for x in sample:
+            p = plans[x]
+            sv = O.statevector(p["n"], O.random_grid_gates(p["r"], p["c"], p["d"], seed=10_000 + p["i"]))
+            ref = sv[[O.amplitude_index(b) for b in p["bits"]]]
+            oracle_errs.append({"circuit": x, "qubits": p["n"], "depth": p["d"], "strategy": p["kind"],
+                                "max_err_over_max_amp": float(np.max(np.abs(amps[x] - ref)) / np.max(np.abs(sv)))})
     secs = sum(ts) / len(ts)
-    kinds = [p["kind"] for p in plans]
     line = {"workload": f"uneven{args.circuits}_random_grid_circuits_64_amplitudes", "precision": prec_name,
-            "metric": "amplitudes/s (all circuits, 64 amplitudes each, compile + graph capture + run + read)",
+            "metric": "amplitudes/s (all circuits, 64 amplitudes each; compiled once, every step replays the "
+                      "captured graphs and reads all amplitudes back)",
             "value": 64 * len(plans) / secs, "unit": "amplitudes/s", "higher_is_better": True,
             "seconds_per_step": secs, "steps": len(ts), "circuits": len(plans),
             "qubits_range": [min(p["n"] for p in plans), max(p["n"] for p in plans)],
             "depth_range": [min(p["d"] for p in plans), max(p["d"] for p in plans)],
-            "strategies": {"statevector": kinds.count("statevector"), "sweep_batched": kinds.count("sweep")},
-            "host_planning_s": t_plan, "network_upload_s": t_build,
+            "strategies": {"statevector_grouped": len(sv_ids), "sweep_batched": len(sw_ids)},
+            "statevector_batch": {**sb_info, "state_budget_gb": args.sv_budget_gb,
+                                  "storage": "complex64 states, FP32 block products"},
+            "kernel_launches_per_step": launches,
+            "host_planning_s": t_plan, "compile_and_upload_s": t_compile, "first_pass_s": t_first,
+            "first_pass_amplitudes_per_s": 64 * len(plans) / (t_compile + t_first),
             "checked_circuits": k, "max_err_over_rms_amplitude_vs_c128": max(errs) if errs else None,
-            "grouping": "one captured graph per circuit, launched in sequence (no cross-circuit kernel batching)",
+            "oracle_sample": oracle_errs,
+            "oracle_max_err_over_max_amp": max(e["max_err_over_max_amp"] for e in oracle_errs) if oracle_errs
+            else None,
+            "grouping": "state-vector circuits: one grouped launch per block index over every circuit of a chunk, "
+                        "the whole batch one CUDA graph; sweep circuits: one captured graph each",
             "data": "synthetic (seeded random circuits)"}
     print(json.dumps(line))
     return 0
@@ -470,7 +546,7 @@ def run_learned(args, rows=7, cols=7, depth=14):
 
     prec_name = args.precision if args.precision != "auto" else "ozaki"
     prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
-            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[prec_name]
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128, "ozaki4": pq.PREC_OZAKI4}[prec_name]
     n = rows * cols
     gates = pq.random_grid_gates(rows, cols, depth, seed=2026)
     bits = pq.random_bitstrings(n, 1, seed=2027)[0]
@@ -603,7 +679,7 @@ def run_pair(args):
 
     M, N, K = (int(x) for x in args.pair.lower().split("x"))
     prec = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
-            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128}[args.precision if args.precision != "auto" else "ozaki"]
+            "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128, "ozaki4": pq.PREC_OZAKI4}[args.precision if args.precision != "auto" else "ozaki"]
     be = pq.GB300Backend(prec)
     rng = np.random.default_rng(0)
     A = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))).astype(np.complex64)
@@ -765,15 +841,15 @@ def run_gb300(args, world, rank):
         dist.init_process_group("nccl")
     dev = torch.cuda.current_device()
     peaks, peaks_kind = load_peaks()
-    prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI, "3xbf16": pq.PREC_3XBF16,
-                "c128": pq.PREC_C128}
+    prec_map = {"c64": pq.PREC_C64, "3xtf32": pq.PREC_3XTF32, "6xtf32": pq.PREC_6XTF32, "ozaki": pq.PREC_OZAKI,
+                "3xbf16": pq.PREC_3XBF16, "c128": pq.PREC_C128, "ozaki4": pq.PREC_OZAKI4}
     prec_name = args.precision if args.precision != "auto" else "ozaki"
     precision = prec_map[prec_name]
 
     if args.workload == "grid6x6_d16_sliced":
         rows, cols, depth = args.rows, args.cols, args.depth
         w = build_sliced(pq, precision, rows, cols, depth, rank=rank, target=args.slice_target,
-                         tuning=args.tuning if precision != pq.PREC_C128 else "off")
+                         tuning=args.tuning if precision != pq.PREC_C128 else "off", storage=args.storage)
         be, plan, sliced = w["be"], w["plan"], w["sliced"]
         if args.batch <= 0:
             args.batch = plan.auto_batch(sliced)
@@ -1007,7 +1083,8 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"c64": "c64", "3xtf32": "c64(3xtf32)", "6xtf32": "c64(6xtf32)",
                                                            "ozaki": "c64(ozaki-bf16)", "3xbf16": "c64(3xbf16)",
-                                                           "c128": "c128"}[prec_name],
+                                                           "c128": "c128", "ozaki4": "c64(ozaki4-bf16)"}[prec_name]
+        if args.storage == "c64" else f"c128({prec_name})",
         "data": "synthetic (seeded random circuits)", "config": workload_config(args, rows, cols, depth),
         "precision": prec_name, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
         "cpu_baseline": cpu,

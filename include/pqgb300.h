@@ -67,13 +67,20 @@ extern "C" {
  *                  five 7-bit bf16 slices, the 15 slice products of level
  *                  <= 4 accumulated in FP32 TMEM where levels 0 and 1 are
  *                  exact; the result is rounded once.  Larger K runs as
- *                  PQ_PREC_6XTF32.                                          */
+ *                  PQ_PREC_6XTF32.
+ * PQ_PREC_OZAKI4 : as PQ_PREC_OZAKI with four slices: the 10 slice products
+ *                  of level <= 3 (residual below 2^-29 of the row / column
+ *                  scale), two thirds of the tensor-core work.  Meant for
+ *                  contexts that store large tensors as complex128
+ *                  (pq_ctx_set_small_elems with a large threshold), where the
+ *                  storage rounding no longer dominates the error.          */
 #define PQ_PREC_C128    0
 #define PQ_PREC_C64     1
 #define PQ_PREC_3XTF32  2
 #define PQ_PREC_3XBF16  3
 #define PQ_PREC_6XTF32  4
 #define PQ_PREC_OZAKI   5
+#define PQ_PREC_OZAKI4  6
 
 #define PQ_MAX_RANK 56
 
@@ -248,6 +255,33 @@ int pq_sliced_result(pq_plan* plan, double* out, int64_t n);
 int pq_plan_profile_sliced(pq_plan* plan, const int64_t* leaf_ids, int n_sliced,
                            const int32_t* sliced_labels, int batch, float* ms,
                            int32_t* batched, double* feats);
+
+/* ---- grouped state vectors of many circuits --------------------------------
+ * An executor beside the pair-plan one for workloads of many circuits, each
+ * asked for a few amplitudes; the reference contracts each circuit alone
+ * (src/layer2.jl:294-321).  Circuit i has n_qubits[i] (<= 31) qubits and
+ * n_blocks[i] blocks, applied in order to |0..0> in a complex64 state (qubit
+ * q at bit q-1 of the amplitude index, the reference's output order
+ * src/layer2.jl:180-189).  Block j (all circuits' blocks concatenated) acts
+ * on block_k[j] (1..4) qubits listed in block_qubits (0-based bit positions,
+ * concatenated; the first is the low bit of the block's matrix index) with
+ * the 2^k x 2^k matrix in block_mats (complex128 interleaved, element
+ * (out, in) at out + in 2^k, concatenated).  Circuit i asks for n_amps[i]
+ * amplitudes at the state indices in amp_idx (concatenated).  Circuits are
+ * packed by size into chunks whose states fit state_budget_bytes (at least
+ * the largest state); launch s of a chunk applies the s-th block of every
+ * circuit in it.  The first execution records every chunk's initialisation,
+ * block launches and amplitude gather as one CUDA graph; executions replay
+ * it and write the amplitudes (complex128 interleaved, in input order). */
+typedef struct pq_svbatch pq_svbatch;
+int pq_svbatch_create(pq_ctx* ctx, int n_circ, const int32_t* n_qubits, const int32_t* n_blocks,
+                      const int32_t* block_k, const int32_t* block_qubits, const double* block_mats,
+                      const int32_t* n_amps, const int64_t* amp_idx, int64_t state_budget_bytes,
+                      pq_svbatch** out);
+int pq_svbatch_execute(pq_svbatch* batch, double* amps_out);
+/* Kernels one execution launches, chunks, and the state arena's bytes. */
+int pq_svbatch_info(pq_svbatch* batch, int64_t* kernel_launches, int64_t* chunks, int64_t* arena_bytes);
+int pq_svbatch_destroy(pq_svbatch* batch);
 
 /* ---- planning ---------------------------------------------------------------
  * Boltzmann-greedy flop-count planner, after src/layer2/bgreedy_contraction.jl:17-66:

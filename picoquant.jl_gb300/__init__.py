@@ -7,7 +7,8 @@ The API keeps PicoQuant's names (Julia's ``!`` dropped):
 backend (the role of ``InteractiveBackend{T}``).  All numeric work runs in
 ``libpqgb300.so`` (CUDA, sm_103a); there is no CPU fallback.
 """
-from ._lib import (PQ_C64, PQ_C128, PQError, PREC_3XBF16, PREC_3XTF32, PREC_6XTF32, PREC_C64, PREC_C128, PREC_OZAKI)
+from ._lib import (PQ_C64, PQ_C128, PQError, PREC_3XBF16, PREC_3XTF32, PREC_6XTF32, PREC_C64, PREC_C128, PREC_OZAKI,
+                   PREC_OZAKI4)
 from .backend import GB300Backend, Metrics, decompose_array, record_compute_costs, record_memory_costs
 from .dsl import DSLBackend, DSLPlan, compile_dsl, execute_dsl_file
 from .mps import (MPSState, calculate_mps_amplitudes, compress_bond, compress_tensor_chain,

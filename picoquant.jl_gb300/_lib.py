@@ -26,6 +26,7 @@ PREC_3XTF32 = 2
 PREC_3XBF16 = 3
 PREC_6XTF32 = 4
 PREC_OZAKI = 5
+PREC_OZAKI4 = 6
 
 PQ_MAX_RANK = 56
 
@@ -111,6 +112,11 @@ SIGNATURES = [
     ("pq_ctx_set_tuning", C.c_int, [vp, C.c_int, C.POINTER(C.c_uint64), i32p]),
     ("pq_ctx_tuning_size", C.c_int, [vp, C.POINTER(C.c_int)]),
     ("pq_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
+    ("pq_svbatch_create", C.c_int, [vp, C.c_int, i32p, i32p, i32p, i32p, f64p, i32p, i64p, C.c_int64,
+                                    C.POINTER(vp)]),
+    ("pq_svbatch_execute", C.c_int, [vp, f64p]),
+    ("pq_svbatch_info", C.c_int, [vp, i64p, i64p, i64p]),
+    ("pq_svbatch_destroy", C.c_int, [vp]),
     ("pq_pair_tuning", C.c_int, [vp, C.c_int, C.c_int, i32p, i64p, C.POINTER(C.c_uint64), C.c_int, i32p,
                                  C.POINTER(C.c_int)]),
 ]

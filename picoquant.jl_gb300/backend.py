@@ -46,7 +46,7 @@ def record_memory_costs(backend, mem):
 
 
 _PREC_NAMES = {L.PREC_C128: "c128", L.PREC_C64: "c64", L.PREC_3XTF32: "3xtf32", L.PREC_3XBF16: "3xbf16",
-               L.PREC_6XTF32: "6xtf32", L.PREC_OZAKI: "ozaki"}
+               L.PREC_6XTF32: "6xtf32", L.PREC_OZAKI: "ozaki", L.PREC_OZAKI4: "ozaki4"}
 
 
 class GB300Backend:

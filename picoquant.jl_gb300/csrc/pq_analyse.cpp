@@ -242,7 +242,7 @@ bool analyse_pair(const std::vector<int>& la, const std::vector<int64_t>& da,
                     (double)G.M * (double)G.N * (double)G.K * (double)G.Z >= double(1 << 20);
   if (gemm_shape &&
       (precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32 || precision == PQ_PREC_OZAKI ||
-       precision == PQ_PREC_3XBF16) &&
+       precision == PQ_PREC_OZAKI4 || precision == PQ_PREC_3XBF16) &&
       tc_eligible(precision, G))
     out.kclass = KC_TC;
   else if (k_both && skinny_eligible(G))

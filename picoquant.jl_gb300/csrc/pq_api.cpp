@@ -115,7 +115,7 @@ extern "C" {
 int pq_ctx_create(int device, int precision, pq_ctx** out) {
   if (!out) return PQ_ERR_INVALID;
   *out = nullptr;
-  if (precision < PQ_PREC_C128 || precision > PQ_PREC_OZAKI) return PQ_ERR_INVALID;
+  if (precision < PQ_PREC_C128 || precision > PQ_PREC_OZAKI4) return PQ_ERR_INVALID;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return PQ_ERR_CUDA;
   pq_ctx* c = new pq_ctx();

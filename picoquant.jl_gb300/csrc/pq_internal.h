@@ -214,7 +214,7 @@ bool tc_eligible(int precision, const GemmDesc& d);
 int tc_launch_count(int precision, const GemmDesc& d);  // kernels one launch_tc issues
 // Exact-accumulation (Ozaki scheme, bf16 slices) tensor-core contraction
 // (pq_oz.cu), used by launch_tc when K <= 512: 5 slices for PQ_PREC_OZAKI,
-// 3 for PQ_PREC_3XBF16.
+// 4 for PQ_PREC_OZAKI4, 3 for PQ_PREC_3XBF16.
 bool oz_eligible(const GemmDesc& d);
 size_t oz_scratch_bytes(int slices, const GemmDesc& d);
 cudaError_t launch_oz(int slices, int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,

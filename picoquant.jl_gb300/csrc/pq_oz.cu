@@ -96,12 +96,13 @@ constexpr int64_t kMaxK = 512;                   // exact level-0/1 sums up to t
 
 // Tile width N: 128 for general pairs, 64 / 32 / 16 for narrow ones.
 // Slices per real value: 5 for PQ_PREC_OZAKI (15 slice pairs, i + j <= 4),
-// 3 for PQ_PREC_3XBF16 (6 pairs, i + j <= 2).
+// 4 for PQ_PREC_OZAKI4 (10 pairs, i + j <= 3), 3 for PQ_PREC_3XBF16 (6
+// pairs, i + j <= 2).
 template <int NSL>
 struct Sl {
-  static_assert(NSL == 5 || NSL == 3, "slice count");
+  static_assert(NSL == 5 || NSL == 4 || NSL == 3, "slice count");
   static constexpr int planes = 2 * NSL;  // per operand: Re s0.., Im s0..
-  static constexpr int pairs = NSL == 5 ? 15 : 6;
+  static constexpr int pairs = NSL == 5 ? 15 : (NSL == 4 ? 10 : 6);
 };
 
 template <int TN, int NSL>
@@ -109,7 +110,7 @@ struct OzCfg {
   static constexpr int kBTile = TN * TK;                                   // bf16 per B plane tile
   static constexpr uint32_t b_bytes = Sl<NSL>::planes * kBTile * 2;        // B planes of one K tile
   static constexpr uint32_t stage_bytes = NSL * kStackBytes + b_bytes;
-  static constexpr int stages = (TN == 128 && NSL == 5) ? 3 : 4;
+  static constexpr int stages = (TN == 128 && NSL >= 4) ? 3 : 4;
   // accumulator sets (three levels of TN columns each): two for TN <= 64, so
   // that the MMAs of the next tile run while the epilogue drains this one
   static constexpr int acc_sets = TN <= 64 ? 2 : 1;
@@ -122,17 +123,20 @@ struct OzCfg {
 // inexact accumulator takes its small terms first).  Five slices:
 //   i: 0 0 1 0 1 2 3 4 0 1 2 3 0 1 2
 //   j: 0 1 0 4 3 2 1 0 3 2 1 0 2 1 0
+// four slices (levels 0 to 3, ten pairs):
+//   i: 0 0 1 0 1 2 3 0 1 2
+//   j: 0 1 0 3 2 1 0 2 1 0
 // three slices:
 //   i: 0 0 1 0 1 2
 //   j: 0 1 0 2 1 0
 // (4-bit fields, pair p in bits [4p, 4p + 4))
 template <int NSL>
 __host__ __device__ constexpr int pair_i(int p) {
-  return (int)((NSL == 5 ? 0x210321043210100ull : 0x210100ull) >> (4 * p)) & 15;
+  return (int)((NSL == 5 ? 0x210321043210100ull : (NSL == 4 ? 0x2103210100ull : 0x210100ull)) >> (4 * p)) & 15;
 }
 template <int NSL>
 __host__ __device__ constexpr int pair_j(int p) {
-  return (int)((NSL == 5 ? 0x12012301234010ull : 0x12010ull) >> (4 * p)) & 15;
+  return (int)((NSL == 5 ? 0x12012301234010ull : (NSL == 4 ? 0x0120123010ull : 0x12010ull)) >> (4 * p)) & 15;
 }
 
 __host__ __device__ constexpr int level_of(int p) { return p == 0 ? 0 : (p < 3 ? 1 : 2); }
@@ -923,7 +927,7 @@ static cudaError_t launch_oz_n(int ta, int tb, int tc, const void* A, const void
 
 cudaError_t launch_oz(int slices, int ta, int tb, int tc, const void* A, const void* B, void* C,
                       const GemmDesc& d0, void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream) {
-  if (!oz_eligible(d0) || (slices != 5 && slices != 3)) return cudaErrorNotSupported;
+  if (!oz_eligible(d0) || (slices != 5 && slices != 4 && slices != 3)) return cudaErrorNotSupported;
   const bool swap = needs_swap(d0);
   const GemmDesc d = swap ? swapped(d0) : d0;
   if (swap) {
@@ -933,8 +937,9 @@ cudaError_t launch_oz(int slices, int ta, int tb, int tc, const void* A, const v
   const OzLayout L = layout(d, slices);
   if (!scratch || scratch_bytes < L.total) return cudaErrorInvalidValue;
   char* base = (char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
-  return slices == 5 ? launch_oz_n<5>(ta, tb, tc, A, B, C, d, base, L, status, stream)
-                     : launch_oz_n<3>(ta, tb, tc, A, B, C, d, base, L, status, stream);
+  if (slices == 5) return launch_oz_n<5>(ta, tb, tc, A, B, C, d, base, L, status, stream);
+  if (slices == 4) return launch_oz_n<4>(ta, tb, tc, A, B, C, d, base, L, status, stream);
+  return launch_oz_n<3>(ta, tb, tc, A, B, C, d, base, L, status, stream);
 }
 
 }  // namespace pq

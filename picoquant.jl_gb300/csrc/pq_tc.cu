@@ -369,18 +369,24 @@ cudaError_t gemm_launch(const float* pa, const float* pb, void* C, const GemmDes
 
 }  // namespace
 
-// PQ_PREC_OZAKI / PQ_PREC_3XBF16 run the exact-accumulation kernels
-// (pq_oz.cu, 5 / 3 bf16 slices) where their limits allow (K <= 512) and the
-// 6xTF32 / 3xTF32 kernels otherwise.
+// PQ_PREC_OZAKI / PQ_PREC_OZAKI4 / PQ_PREC_3XBF16 run the exact-accumulation
+// kernels (pq_oz.cu, 5 / 4 / 3 bf16 slices) where their limits allow
+// (K <= 512) and the 6xTF32 (the first two) / 3xTF32 kernels otherwise.
 static bool tf32_eligible(const GemmDesc& d) {
   if (d.M < 64 || d.N < 64 || d.K < 16) return false;
   return d.Z <= 65535 && ceil_div(d.N, TN) <= 65535 && ceil_div(d.M, TM) <= 65535;
 }
 static int tf32_precision(int precision) {
-  return precision == PQ_PREC_OZAKI ? PQ_PREC_6XTF32 : (precision == PQ_PREC_3XBF16 ? PQ_PREC_3XTF32 : precision);
+  return (precision == PQ_PREC_OZAKI || precision == PQ_PREC_OZAKI4)
+             ? PQ_PREC_6XTF32
+             : (precision == PQ_PREC_3XBF16 ? PQ_PREC_3XTF32 : precision);
 }
-static bool sliced_bf16(int precision) { return precision == PQ_PREC_OZAKI || precision == PQ_PREC_3XBF16; }
-static int bf16_slices(int precision) { return precision == PQ_PREC_OZAKI ? 5 : 3; }
+static bool sliced_bf16(int precision) {
+  return precision == PQ_PREC_OZAKI || precision == PQ_PREC_OZAKI4 || precision == PQ_PREC_3XBF16;
+}
+static int bf16_slices(int precision) {
+  return precision == PQ_PREC_OZAKI ? 5 : (precision == PQ_PREC_OZAKI4 ? 4 : 3);
+}
 
 size_t tc_scratch_bytes(int precision, const GemmDesc& d) {
   if (sliced_bf16(precision) && oz_eligible(d)) return oz_scratch_bytes(bf16_slices(precision), d);

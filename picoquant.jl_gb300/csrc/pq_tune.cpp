@@ -24,10 +24,12 @@ int ceil_log2(int64_t x) {
 
 bool tc_precision(int precision) {
   return precision == PQ_PREC_3XTF32 || precision == PQ_PREC_6XTF32 || precision == PQ_PREC_OZAKI ||
-         precision == PQ_PREC_3XBF16;
+         precision == PQ_PREC_OZAKI4 || precision == PQ_PREC_3XBF16;
 }
 
-bool sliced_precision(int precision) { return precision == PQ_PREC_OZAKI || precision == PQ_PREC_3XBF16; }
+bool sliced_precision(int precision) {
+  return precision == PQ_PREC_OZAKI || precision == PQ_PREC_OZAKI4 || precision == PQ_PREC_3XBF16;
+}
 
 bool same(const TuneChoice& a, const TuneChoice& b) {
   return a.kclass == b.kclass && a.tile_n == b.tile_n && a.orient == b.orient;

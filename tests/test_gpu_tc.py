@@ -415,3 +415,51 @@ def test_ozaki_stride1_mode_contracted(pq, O, ia):
     assert nl == OZ_LAUNCHES
     ref = O.contract_tensors_arrays(A.astype(np.complex128), ia, B.astype(np.complex128), ib)
     assert rel_err(got, ref) < 3e-7
+
+
+@pytest.mark.parametrize("small", [1 << 16, 1 << 62], ids=["c64-storage", "c128-storage"])
+def test_ozaki4_matches_cpu_restatement(pq, small):
+    """Four bf16 slices (PQ_PREC_OZAKI4, ten slice-pair products): the device
+    result is the CPU restatement with n_slices = 4 up to the FP32 sum of the
+    small levels and the output rounding, and the FP64 product within the
+    scheme's bound; with every tensor stored as complex128 the result is not
+    rounded to complex64 at all."""
+    from oracle import ozaki_oracle as Z
+
+    rng = np.random.default_rng(12)
+    A = rand(rng, (384, 256))
+    B = rand(rng, (256, 200))
+    if small < (1 << 62):
+        A = A.astype(np.complex64).astype(np.complex128)
+    be = pq.GB300Backend(pq.PREC_OZAKI4, small_elems=small)
+    got, nl = run(be, A, [-1, 1], B, [1, -2])
+    be.close()
+    assert nl == OZ_LAUNCHES
+    orc, _ = Z.ozaki_matmul(A, B, n_slices=4)
+    ref = A @ B
+    bound = Z.error_bound(A, B, ref, n_slices=4)
+    assert np.all(np.abs(got - ref) <= bound)
+    na = np.sqrt(np.sum(np.abs(A) ** 2, axis=1))
+    nb = np.sqrt(np.sum(np.abs(B) ** 2, axis=0))
+    tol = (2.0 ** -23 * np.abs(orc) if small < (1 << 62) else 0) + 2.0 ** -28 * np.outer(na, nb)
+    assert np.all(np.abs(got - orc) <= tol)
+
+
+def test_ozaki4_c128_plan_amplitude(pq, O):
+    """A sliced amplitude with four slices and complex128 storage against
+    the state vector: the error is far below the complex64-storage modes'."""
+    be = pq.GB300Backend(pq.PREC_OZAKI4, small_elems=1 << 62)
+    r, c, d = 4, 4, 10
+    bits = "0110100111001010"
+    g = pq.random_grid_gates(r, c, d, seed=3)
+    net = pq.build_network(16, g, backend=be, decompose=True)
+    pq.add_input(net, "0" * 16)
+    pq.add_output(net, bits)
+    steps, cm, mx, _ = pq.planning.best_flop_plan(net, out_edges=[], candidates=("sweep",))
+    plan = pq.NetworkPlan(net, steps=steps, out_edges=[])
+    sliced = plan.choose_slices(max_sliced=4, log2_target=28)
+    amp = plan.run_sliced(sliced, batch=16)
+    ref = O.statevector(16, g)[O.amplitude_index(bits)]
+    assert abs(amp - ref) / 2.0 ** -8 < 1e-7
+    plan.close()
+    be.close()
