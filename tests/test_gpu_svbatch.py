@@ -54,15 +54,16 @@ def test_svbatch_matches_oracle(pq, O):
 
 
 def test_svbatch_chunks_give_the_same_amplitudes(pq, O):
-    """A budget of one 2^14-amplitude state forces one chunk per circuit
-    (largest first); the amplitudes are bit-identical to one chunk's."""
+    """A budget of one 2^14-amplitude state splits the batch: the 14-qubit
+    circuit alone, then every smaller one (2^13 + 2^12 + ... fits); the
+    amplitudes are bit-identical to one chunk's."""
     from pqgb300.svbatch import StateVectorBatch
 
     circs, raw = _circuits(pq, SPECS)
     be = pq.GB300Backend(pq.PREC_C64)
     one = StateVectorBatch(be, circs).execute()
     sb = StateVectorBatch(be, circs, state_budget_bytes=8 << 14)
-    assert sb.info()["chunks"] == len(SPECS)
+    assert sb.info()["chunks"] == 2
     many = sb.execute()
     for a, b in zip(one, many):
         assert np.array_equal(a, b)
