@@ -70,10 +70,12 @@ extern "C" {
  *                  PQ_PREC_6XTF32.
  * PQ_PREC_OZAKI4 : as PQ_PREC_OZAKI with four slices: the 10 slice products
  *                  of level <= 3 (residual below 2^-29 of the row / column
- *                  scale), two thirds of the tensor-core work.  Meant for
- *                  contexts that store large tensors as complex128
- *                  (pq_ctx_set_small_elems with a large threshold), where the
- *                  storage rounding no longer dominates the error.          */
+ *                  scale), two thirds of the tensor-core work.  With
+ *                  complex64 storage its added error is about the size of the
+ *                  storage rounding (amplitude errors about twice
+ *                  PQ_PREC_OZAKI's); complex128 storage (pq_ctx_set_small_elems
+ *                  with a large threshold) removes the storage rounding but
+ *                  runs the memory-bound steps in FP64.                     */
 #define PQ_PREC_C128    0
 #define PQ_PREC_C64     1
 #define PQ_PREC_3XTF32  2
@@ -285,9 +287,11 @@ int pq_svbatch_destroy(pq_svbatch* batch);
 
 /* ---- planning ---------------------------------------------------------------
  * Boltzmann-greedy flop-count planner, after src/layer2/bgreedy_contraction.jl:17-66:
- * pairs are sampled with weight exp(-(cost - best)/tau) where
- * cost = log2|C| - alpha*log2(|A|+|B|) style heuristic over pairs that share
- * a label (then disjoint pieces by outer product); `n_trials` plans are drawn
+ * pairs that share a label (then disjoint pieces by outer product) are scored
+ * by the Gray-Kourtis energy cost = |C| - alpha (|A| + |B|) (tensor sizes in
+ * elements, bgreedy_contraction.jl:76-94) and sampled with weight
+ * exp(-(cost - best) / (tau max(1, |best|))) (a temperature relative to the
+ * best pair's cost; tau = 0 takes the best pair); `n_trials` plans are drawn
  * and the one with the fewest complex multiply-adds is kept.  Writes
  * 2*(n_leaves-1) SSA operands into `steps` and returns its cost in `cmacs`
  * and its largest intermediate in `max_elems`.  Labels in `out_labels` are
