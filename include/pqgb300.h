@@ -320,6 +320,18 @@ int pq_plan_greedy_many(int n_leaves, const int32_t* leaf_ranks, const int32_t* 
 int pq_plan_cost(int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels, int n_labels,
                  const int64_t* label_dims, int n_steps, const int32_t* steps, int n_out,
                  const int32_t* out_labels, double* cmacs, double* max_elems);
+/* pq_plan_cost for n_cand candidate plans of the same leaves at once, on the
+ * context's device (the candidate scoring of the planners: seeded greedy
+ * draws after src/layer2/bgreedy_contraction.jl:17-131, randomized sweeps):
+ * steps holds n_cand x 2 n_steps SSA operands, candidate after candidate;
+ * cmacs[c] and max_elems[c] are plan c's values.  One warp per candidate
+ * with its label counts in shared memory (at most 40000 labels, leaf ranks
+ * at most 64).  A candidate with an intermediate of more than 64 labels gets
+ * infinite values; one that is not an SSA plan of the leaves makes the call
+ * fail with PQ_ERR_INVALID. */
+int pq_plan_cost_batch(pq_ctx* ctx, int n_leaves, const int32_t* leaf_ranks, const int32_t* leaf_labels,
+                       int n_labels, const int64_t* label_dims, int n_steps, int n_cand, const int32_t* steps,
+                       int n_out, const int32_t* out_labels, double* cmacs, double* max_elems);
 /* Choose labels to slice: repeatedly fix the label that most reduces the
  * largest intermediate (ties: least flop increase) until the largest
  * intermediate is <= 2^log2_target elements or `max_sliced` labels are

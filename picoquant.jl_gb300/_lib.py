@@ -117,6 +117,8 @@ SIGNATURES = [
     ("pq_svbatch_execute", C.c_int, [vp, f64p]),
     ("pq_svbatch_info", C.c_int, [vp, i64p, i64p, i64p]),
     ("pq_svbatch_destroy", C.c_int, [vp]),
+    ("pq_plan_cost_batch", C.c_int, [vp, C.c_int, i32p, i32p, C.c_int, i64p, C.c_int, C.c_int, i32p, C.c_int, i32p,
+                                     f64p, f64p]),
     ("pq_pair_tuning", C.c_int, [vp, C.c_int, C.c_int, i32p, i64p, C.POINTER(C.c_uint64), C.c_int, i32p,
                                  C.POINTER(C.c_int)]),
 ]

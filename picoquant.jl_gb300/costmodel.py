@@ -20,8 +20,8 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib as L
-from .planning import (NetworkPlan, _leaf_arrays, greedy_draws, open_output_edges, plan_cost, sweep_steps,
-                       wavefunction_steps)
+from .planning import (NetworkPlan, _leaf_arrays, device_backend, greedy_draws, open_output_edges, plan_cost,
+                       sweep_steps, wavefunction_steps)
 
 N_FEATURES = 5
 WEIGHTS_FILE = Path(__file__).resolve().parent / "costmodel_gb300.npz"
@@ -252,7 +252,8 @@ def candidate_plans(network, out_edges=None, n_random=16, seed=0, n_sweep_random
     # the sweep and native greedy planners return their own cost and largest
     # intermediate (the same label rule as plan_cost)
     for i, (s, c, m) in enumerate(sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, all_orders=True,
-                                              random_orders=n_sweep_random, seed=seed)):
+                                              random_orders=n_sweep_random, seed=seed,
+                                              cost_backend=device_backend(network))):
         out.append({"name": f"sweep{i}", "steps": s, "cmacs": c, "max_elems": m})
     if not out_edges or all(network.edges[e].src is not None for e in network.input_qubits):
         try:

@@ -402,6 +402,38 @@ def plan_cost(ranks, flat, dims, steps, out_labels):
     return cm.value, mx.value
 
 
+def device_backend(network):
+    """The network's backend when it has a device context (candidate plans
+    are then scored on the device), else None."""
+    be = network.backend
+    return be if getattr(be, "ctx", None) is not None and hasattr(be, "lib") else None
+
+
+def plan_cost_batch(backend, ranks, flat, dims, step_lists, out_labels):
+    """(cmacs, max_elems) of many SSA plans of the same leaves, scored on the
+    backend's device in one launch (``pq_plan_cost_batch``: one warp per
+    plan, the executor's label rule); the values of ``plan_cost``."""
+    lib = L.lib()
+    n = len(step_lists)
+    if n == 0:
+        return []
+    ns = len(step_lists[0]) // 2
+    if any(len(st) != 2 * ns for st in step_lists):
+        raise ValueError("plans of one network have the same number of steps")
+    st = np.ascontiguousarray(np.asarray(step_lists, dtype=np.int32).reshape(-1) if ns else np.zeros(1, np.int32))
+    a32 = [np.ascontiguousarray(np.asarray(v, dtype=np.int64).reshape(-1), dtype=np.int32)
+           if len(v) else np.zeros(1, np.int32) for v in (ranks, flat, out_labels)]
+    d64 = np.ascontiguousarray(np.asarray(dims, dtype=np.int64).reshape(-1)) if len(dims) else np.zeros(1, np.int64)
+    cm = np.empty(n, np.float64)
+    mx = np.empty(n, np.float64)
+    rc = lib.pq_plan_cost_batch(backend.ctx, len(ranks), a32[0].ctypes.data_as(L.i32p), a32[1].ctypes.data_as(L.i32p),
+                                len(dims), d64.ctypes.data_as(L.i64p), ns, n, st.ctypes.data_as(L.i32p),
+                                len(out_labels), a32[2].ctypes.data_as(L.i32p), cm.ctypes.data_as(L.f64p),
+                                mx.ctypes.data_as(L.f64p))
+    L.check(rc, backend.ctx, "pq_plan_cost_batch")
+    return list(zip(cm.tolist(), mx.tolist()))
+
+
 def _node_qubit(network, node_label):
     for idx in network.nodes[node_label].indices:
         e = network.edges.get(idx)
@@ -411,7 +443,7 @@ def _node_qubit(network, node_label):
 
 
 def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None, flat=None, dims=None,
-                all_orders=False, random_orders=0, keep_random=4, seed=0):
+                all_orders=False, random_orders=0, keep_random=4, seed=0, cost_backend=None):
     """Qubit-sweep plan: contract each qubit's tensors along time into one
     tensor, then absorb qubits one at a time into a growing boundary.
 
@@ -422,7 +454,9 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
     the frontier, T cycling through 0.3, 0.7, 1.5 in log2 elements), of which
     the ``keep_random`` cheapest are kept.  The cheapest by complex
     multiply-adds is returned as (steps, cmacs, max_elems), or every kept
-    order's triple when ``all_orders``.
+    order's triple when ``all_orders``.  With ``cost_backend`` (a backend with
+    a device context) the candidates are scored together on the device
+    (``plan_cost_batch``).
     """
     leaves = leaves if leaves is not None else list(network.nodes.keys())
     groups: dict[int, list] = {}
@@ -545,22 +579,27 @@ def sweep_steps(network, leaves=None, out_labels=None, label_of=None, ranks=None
             n2 += 1
         return steps
 
-    found = []
-    for order in orders:
-        steps = order_steps(order)
-        found.append((steps, *plan_cost(ranks, flat, dims, steps, out_labels)))
+    def costs(step_lists):
+        # every candidate's (cmacs, max_elems): one device batch when a
+        # backend context is given, else one native host pass each
+        if cost_backend is not None and len(step_lists) > 1:
+            return plan_cost_batch(cost_backend, ranks, flat, dims, step_lists, out_labels)
+        return [plan_cost(ranks, flat, dims, st, out_labels) for st in step_lists]
+
+    step_lists = [order_steps(order) for order in orders]
+    found = [(st, *cm) for st, cm in zip(step_lists, costs(step_lists))]
     if random_orders > 0:
         rng = np.random.default_rng(seed)
         temps = (0.3, 0.7, 1.5)
         seen = {tuple(o) for o in orders}
-        extra = []
+        extra_steps = []
         for i in range(random_orders):
             o = greedy_order(qs[int(rng.integers(nq))], rng, temps[i % len(temps)])
             if tuple(o) in seen:
                 continue
             seen.add(tuple(o))
-            steps = order_steps(o)
-            extra.append((steps, *plan_cost(ranks, flat, dims, steps, out_labels)))
+            extra_steps.append(order_steps(o))
+        extra = [(st, *cm) for st, cm in zip(extra_steps, costs(extra_steps))]
         extra.sort(key=lambda t: (t[1], t[2]))
         found += extra[:keep_random]
     if all_orders:
@@ -585,7 +624,7 @@ def best_flop_plan(network, out_edges=None, trials=16, seed=0, candidates=("swee
         found.append((s, *plan_cost(ranks, flat, dims, s, outl), "greedy"))
     if "sweep" in candidates:
         s, c, m = sweep_steps(network, nodes, outl, label_of, ranks, flat, dims, random_orders=sweep_random,
-                              seed=seed)
+                              seed=seed, cost_backend=device_backend(network))
         found.append((s, c, m, "sweep"))
     if "wavefunction" in candidates and all(network.edges[e].src is not None for e in network.input_qubits):
         try:

@@ -380,3 +380,36 @@ def test_grid7x7_d14_amplitude_vs_oracle(pq, O):
     assert abs(amp_s - ref) <= 1e-6 * abs(ref), (amp_s, ref, sizes)
     plan.close()
     be.close()
+
+
+@pytest.mark.parametrize("rows,cols,depth", [(5, 5, 12), (7, 7, 14)])
+def test_plan_cost_batch_matches_host(pq, rows, cols, depth):
+    """Candidate scoring on the device (one warp per plan) gives the host
+    pass's complex multiply-adds and largest intermediate for seeded greedy
+    draws and qubit-sweep orders of a decomposed random circuit, and the
+    sweep planner picks the same plan with device scoring; a plan that is not
+    SSA over the leaves is refused."""
+    from pqgb300 import _lib as L
+    from pqgb300 import planning as PL
+
+    n = rows * cols
+    be = pq.GB300Backend(pq.PREC_C64)
+    net = pq.build_network(n, pq.random_grid_gates(rows, cols, depth, seed=8), decompose=True, backend=be)
+    pq.add_input(net, "0" * n)
+    pq.add_output(net, pq.random_bitstrings(n, 1, seed=9)[0])
+    nodes, ranks, flat, dims, label_of = PL._leaf_arrays(net, [])
+    cands = [s for s, _, _ in PL.greedy_draws(ranks, flat, dims, [], 24, seed=3)]
+    cands += [s for s, _, _ in PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, all_orders=True,
+                                              random_orders=16, seed=1)]
+    got = PL.plan_cost_batch(be, ranks, flat, dims, cands, [])
+    for st, (cm, mx) in zip(cands, got):
+        hc, hm = PL.plan_cost(ranks, flat, dims, st, [])
+        assert abs(cm - hc) <= 1e-9 * hc and abs(mx - hm) <= 1e-9 * hm
+    host = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, random_orders=16, seed=1)
+    dev = PL.sweep_steps(net, nodes, [], label_of, ranks, flat, dims, random_orders=16, seed=1, cost_backend=be)
+    assert dev[0] == host[0] and abs(dev[1] - host[1]) <= 1e-9 * host[1]
+    bad = list(cands[0])
+    bad[0] = len(nodes) + 5  # an operand that does not exist yet
+    with pytest.raises(L.PQError):
+        PL.plan_cost_batch(be, ranks, flat, dims, [cands[1], bad], [])
+    be.close()
