@@ -157,18 +157,8 @@ __device__ __forceinline__ float absmax(float a, float b) { return fmaxf(fabsf(a
 __device__ __forceinline__ double absmax(double a, double b) { return fmax(fabs(a), fabs(b)); }
 __device__ __forceinline__ float scale2(float x, int e) { return ldexpf(x, e); }
 __device__ __forceinline__ double scale2(double x, int e) { return ldexp(x, e); }
-// Round to the nearest integer, ties to even, for |x| < 2^22 (float) /
-// 2^51 (double) -- the slices' range (|x| <= 2^7): adding and subtracting
-// 1.5 2^23 (1.5 2^52) rounds x at the unit place in the FMA pipe (the
-// additions are not reassociated), the same value as rintf / rint.
-__device__ __forceinline__ float round_int(float x) {
-  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-  return __fsub_rn(__fadd_rn(x, kMagic), kMagic);
-}
-__device__ __forceinline__ double round_int(double x) {
-  constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
-  return __dsub_rn(__dadd_rn(x, kMagic), kMagic);
-}
+__device__ __forceinline__ float round_int(float x) { return rintf(x); }
+__device__ __forceinline__ double round_int(double x) { return rint(x); }
 
 __device__ __forceinline__ int exp_of(float v) {
   int e;
