@@ -541,8 +541,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // byte offset of (slice 0, block 0, row r, K value kq) in the stacks
     const uint32_t row_off = (uint32_t)((((kq >> 3) * 24 + (r >> 3)) * 8 + (r & 7)) * 16 + (kq & 7) * 2);
     // This CTA's K tiles form one sequence g = tile number * ktiles + kt; the
-    // group takes g = grp, grp + H, ...  The next two's A values and row
-    // exponents are loaded while this one is sliced, across tile boundaries
+    // group takes g = grp, grp + H, ...  The next one's A values and row
+    // exponent are loaded while this one is sliced, across tile boundaries
     // (a tile's rows and exponent are looked up once per tile).
     const int64_t ntl = blockIdx.x < ntot ? (ntot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const int64_t items = ntl * ktiles;
@@ -573,28 +573,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     };
-    // two of the group's K tiles in flight while one is sliced: n1 (the
-    // next) and n2 (the one after), each with its row exponent
-    TA n1[NV], n2[NV];
-    int e1 = kExpZero, e2 = kExpZero;
-    auto fetch = [&](int64_t g, TA* v, int& ev) {
-      const int64_t tl = g / ktiles;
-      if (tl != ptl) row_info(tl);
-      ev = en;
-      load(g - tl * ktiles, v);
-    };
-    if (grp < items) fetch(grp, n1, e1);
-    if (grp + H < items) fetch(grp + H, n2, e2);
+    TA nxt[NV];
+    if (grp < items) {
+      row_info(grp / ktiles);
+      load(grp % ktiles, nxt);
+    }
     for (int64_t gk = grp; gk < items && ok; gk += H) {
-      const int e = e1;
+      const int e = en;
       TA cur[NV];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) {
-        cur[q] = n1[q];
-        n1[q] = n2[q];
+      for (int q = 0; q < NV; ++q) cur[q] = nxt[q];
+      if (gk + H < items) {  // in flight while this K tile is sliced
+        const int64_t gp = gk + H, tl = gp / ktiles;
+        if (tl != ptl) row_info(tl);
+        load(gp - tl * ktiles, nxt);
       }
-      e1 = e2;
-      if (gk + 2 * H < items) fetch(gk + 2 * H, n2, e2);
       const float2 f = inv_scale(e != kExpZero ? e : 0);
       {
         const int s = (int)(gk % kStages);
