@@ -14,8 +14,10 @@ eligible choice -- kernel class, and for the exact-accumulation tensor-core
 class a tile width of 16 to 128 columns and an orientation -- is timed by the
 library's own harness (``pq_measure_pairs``, CUDA events, random operands of
 the pair's shape), the default included: one quick pass over all choices,
-then ``reps`` timed runs of the three fastest.  The fastest is installed in
-the context (``pq_ctx_set_tuning``), which every later contraction, plan
+then ``reps`` timed runs of the three fastest and the default.  The fastest
+replaces the default only when it is at least 5 % faster (closer timings are
+noise, and a change of kernel class can change the rounding); the choice is
+installed in the context (``pq_ctx_set_tuning``), which every later contraction, plan
 compile and measurement on it consults, and the table is persisted as JSON
 keyed by the GPU's name and a hash of the kernel sources (a cache written for
 other kernels or another GPU is ignored).
@@ -98,8 +100,9 @@ def plan_pairs(plan):
 class Tuner:
     """Per-class tuned choices for one backend context (see the module doc)."""
 
-    def __init__(self, backend):
+    def __init__(self, backend, margin=0.05):
         self.be = backend
+        self.margin = margin  # a choice must beat the default by this fraction to replace it
         self.entries: dict[int, dict] = {}
 
     # ---- library calls ------------------------------------------------------
@@ -144,6 +147,8 @@ class Tuner:
             best.append(cands[0])  # the default is always re-timed
         timed = {c: self._time(key, c, shape, reps) for c in best}
         win = min(timed, key=timed.get)
+        if timed[win] > (1.0 - self.margin) * timed[cands[0]]:
+            win = cands[0]  # within the timing noise: keep the fixed rule's choice
         self.entries[key] = {"choice": list(win), "default": list(cands[0]),
                              "ms": {choice_name(c): t for c, t in timed.items()},
                              "shape": {"a": [int(x) for x in da], "b": [int(x) for x in db],
