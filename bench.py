@@ -427,15 +427,21 @@ def run_uneven(args):
             sweeps.append((k, plan, out))
         return (sb, list(ids_sv)), sweeps
 
+    split = {"statevector_s": [], "sweeps_s": []}
+
     def run_all(be, sbk, sweeps):
         amps = {}
         sb, keys = sbk
+        t_a = time.perf_counter()
         if sb is not None:
             for k, a in zip(keys, sb.execute()):
                 amps[k] = a
+        t_b = time.perf_counter()
         for k, plan, out in sweeps:
             plan.execute(out)
             amps[k] = np.asarray(be.load_tensor_data(out)).reshape(-1)
+        split["statevector_s"].append(t_b - t_a)
+        split["sweeps_s"].append(time.perf_counter() - t_b)
         return amps
 
     budget = int(args.sv_budget_gb * (1 << 30))
@@ -457,6 +463,15 @@ def run_uneven(args):
         ts.append(time.perf_counter() - t1)
     launches = (be.launch_count() - launches0) / max(1, args.steps)
     sb_info = sb.info() if sb is not None else {}
+    n_t = max(1, args.steps)
+    t_sv = float(np.mean(split["statevector_s"][-n_t:]))
+    t_swp = float(np.mean(split["sweeps_s"][-n_t:]))
+    if sb is not None:
+        peaks, peaks_kind = load_peaks()
+        sb_info.update({"seconds_per_step": t_sv, "algorithmic_bytes": sb.algorithmic_bytes,
+                        "achieved_gbs": sb.algorithmic_bytes / t_sv / 1e9,
+                        "frac_of_hbm": sb.algorithmic_bytes / t_sv / 1e9 / peaks["hbm_gbs"],
+                        "hbm_peak_source": f"{peaks_kind} hbm copy"})
     if sb is not None:
         sb.close()
     for _, plan, _ in sweeps:
@@ -515,7 +530,7 @@ def run_uneven(args):
             "strategies": {"statevector_grouped": len(sv_ids), "sweep_batched": len(sw_ids)},
             "statevector_batch": {**sb_info, "state_budget_gb": args.sv_budget_gb,
                                   "storage": "complex64 states, FP32 block products"},
-            "kernel_launches_per_step": launches,
+            "kernel_launches_per_step": launches, "sweep_circuits_seconds_per_step": t_swp,
             "host_planning_s": t_plan, "compile_and_upload_s": t_compile, "first_pass_s": t_first,
             "first_pass_amplitudes_per_s": 64 * len(plans) / (t_compile + t_first),
             "checked_circuits": k, "max_err_over_rms_amplitude_vs_c128": max(errs) if errs else None,

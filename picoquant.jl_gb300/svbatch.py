@@ -52,6 +52,9 @@ class StateVectorBatch:
             na.append(len(bitstrings))
             idx += [bitstring_index(b) for b in bitstrings]
         self.n_amps = na
+        # bytes one execution moves at least: every block pass reads and
+        # writes its circuit's whole complex64 state once
+        self.algorithmic_bytes = sum(16 * (1 << int(n)) * len(blocks) for n, blocks, _ in circuits)
         mats = np.concatenate(mats) if mats else np.zeros(2)
         a32 = lambda v: np.ascontiguousarray(v if len(v) else [0], dtype=np.int32)
         arrs = [a32(nq), a32(nb), a32(nk), a32(qbits)]
