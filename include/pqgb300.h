@@ -165,6 +165,25 @@ int pq_reshape_tensor(pq_ctx* ctx, int64_t id, int n_groups, const int32_t* grou
  * narrowed to the 1-based inclusive range lo1:hi1. */
 int pq_view_tensor(pq_ctx* ctx, int64_t view_id, int64_t node, int bond_idx1,
                    int64_t lo1, int64_t hi1);
+/* src/backends/interactive.jl:124-151 -> src/layer1.jl:146-184
+ * (`decompose_tensor!`): splits tensor `id` by SVD into
+ *   left_id  with dims (left dims..., chi)  and
+ *   right_id with dims (chi, right dims...),
+ * each factor carrying sqrt(S), as in the reference.  `left1`/`right1` are
+ * 1-based axis numbers that together name every axis once.  chi counts the
+ * singular values with s / ||s||_2 > max(threshold, sqrt(eps)) (eps of
+ * ComplexF32, or of ComplexF64 in a PQ_PREC_C128 context), capped by
+ * max_rank when max_rank > 0; it is written to *chi_out.  The input is
+ * deleted.  The SVD is one-sided Jacobi on the device (one CTA), in complex
+ * FP64 in a PQ_PREC_C128 context and in complex FP32 otherwise (LAPACK's
+ * precision for the reference's ComplexF64 / ComplexF32 backends); the
+ * smaller of the two matrix sides is limited to 256 and the product of the
+ * sides to 2^24 (PQ_ERR_UNSUPPORTED beyond).  *sweeps_out (may be NULL)
+ * receives the number of Jacobi sweeps taken (at most 60). */
+int pq_decompose_tensor(pq_ctx* ctx, int64_t id, int n_left, const int32_t* left1,
+                        int n_right, const int32_t* right1, double threshold,
+                        int max_rank, int64_t left_id, int64_t right_id, int* chi_out,
+                        int* sweeps_out);
 /* Gather amplitudes: out[i] = T[idx[i]] for linear (column-major) indices,
  * written as `dtype` into host memory.  Synchronises. */
 int pq_gather_elements(pq_ctx* ctx, int64_t id, const int64_t* idx, int64_t n,

@@ -64,7 +64,11 @@ class GB300Backend:
     the error of the final amplitudes.
     """
 
-    def __init__(self, precision: int = L.PREC_C64, device: int = 0, small_elems: int | None = None):
+    def __init__(self, precision: int = L.PREC_C64, device: int = 0, small_elems: int | None = None,
+                 svd: str = "host"):
+        if svd not in ("host", "device"):
+            raise ValueError(f"svd must be 'host' or 'device', not {svd!r}")
+        self.svd = svd
         self.lib = L.lib()
         h = C.c_void_p()
         rc = self.lib.pq_ctx_create(device, precision, C.byref(h))
@@ -239,9 +243,23 @@ class GB300Backend:
                          left_label=None, right_label=None):
         """src/backends/interactive.jl:124-151 -> src/layer1.jl:146-184.
 
-        The SVD split is not on the contraction path; it runs on the host in
-        FP64 and the two factors are uploaded.  Returns the new bond extent.
+        The SVD split is not on the contraction path.  With ``svd="host"``
+        (the default) the tensor is downloaded, split by LAPACK in FP64 and
+        the two factors uploaded; with ``svd="device"`` it is split in place
+        by the library's one-sided Jacobi SVD (FP64, one CTA; the smaller
+        side of the split at most 256).  Returns the new bond extent.
         """
+        if self.svd == "device":
+            lp = np.ascontiguousarray(left_positions, dtype=np.int32)
+            rp = np.ascontiguousarray(right_positions, dtype=np.int32)
+            chi, sweeps = C.c_int(0), C.c_int(0)
+            rc = self.lib.pq_decompose_tensor(self.ctx, self.id_of(tensor), lp.size, lp.ctypes.data_as(L.i32p),
+                                              rp.size, rp.ctypes.data_as(L.i32p), float(threshold), int(max_rank),
+                                              self.id_of(left_label), self.id_of(right_label), C.byref(chi),
+                                              C.byref(sweeps))
+            self._check(rc, f"decompose_tensor({tensor})")
+            self.last_svd_sweeps = sweeps.value
+            return chi.value
         data = self.load_tensor_data(tensor)
         B, Cm, chi = decompose_array(data, left_positions, right_positions, threshold, max_rank,
                                      eps_dtype=np.float32 if self.precision != L.PREC_C128 else np.float64)

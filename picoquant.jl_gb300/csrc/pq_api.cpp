@@ -3,6 +3,7 @@
 // Mirrors the method table of the reference's InteractiveBackend
 // (src/backends/interactive.jl:10-172) with device-resident tensors.
 #include <algorithm>
+#include <cmath>
 #include <complex>
 #include <cstring>
 #include <vector>
@@ -504,6 +505,134 @@ int pq_reshape_tensor(pq_ctx* c, int64_t id, int n_groups, const int32_t* group_
   }
   if (prod(nd) != T.size) return fail(ctx, PQ_ERR_INVALID, "reshape_tensor: size changes");
   T.dims = nd;
+  return PQ_OK;
+}
+
+int pq_decompose_tensor(pq_ctx* c, int64_t id, int n_left, const int32_t* left1, int n_right, const int32_t* right1,
+                        double threshold, int max_rank, int64_t left_id, int64_t right_id, int* chi_out,
+                        int* sweeps_out) {
+  CTX_OR_FAIL(c);
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "decompose_tensor: no tensor " + std::to_string(id));
+  const Tensor& T = it->second;
+  const int rank = (int)T.dims.size();
+  if (n_left < 0 || n_right < 0 || n_left + n_right != rank || (n_left && !left1) || (n_right && !right1) ||
+      !chi_out || left_id == right_id || left_id == id || right_id == id || max_rank < 0)
+    return fail(ctx, PQ_ERR_INVALID, "decompose_tensor: bad arguments");
+  std::vector<int> seen(rank, 0), perm(rank);
+  std::vector<int64_t> ld, rd;
+  int64_t m = 1, n = 1;
+  for (int i = 0; i < rank; ++i) {
+    const int p = (i < n_left ? left1[i] : right1[i - n_left]) - 1;
+    if (p < 0 || p >= rank || seen[p]) return fail(ctx, PQ_ERR_INVALID, "decompose_tensor: positions not a permutation");
+    seen[p] = 1;
+    perm[i] = p;
+    (i < n_left ? ld : rd).push_back(T.dims[p]);
+    (i < n_left ? m : n) *= T.dims[p];
+  }
+  const int64_t R = m < n ? n : m;
+  const int64_t Cn = m < n ? m : n;
+  if (Cn > 256 || R * Cn > (int64_t(1) << 24))
+    return fail(ctx, PQ_ERR_UNSUPPORTED, "decompose_tensor: the device SVD takes at most 256 columns and 2^24 "
+                                         "elements (the smaller side of the split is " + std::to_string(Cn) + ")");
+  // arithmetic of the context's element type, as LAPACK's for the reference
+  // backend's T: complex FP64 in complex128 contexts, complex FP32 otherwise
+  const int wt = ctx->precision == PQ_PREC_C128 ? PQ_C128 : PQ_C64;
+  const size_t csz = wt == PQ_C128 ? 16 : 8, rsz = csz / 2;
+  // the matrix A (m x n, column-major): the tensor permuted to (left..., right...)
+  std::vector<int> la(rank), lc(rank);
+  for (int i = 0; i < rank; ++i) la[i] = i;
+  for (int i = 0; i < rank; ++i) lc[i] = perm[i];
+  PairPlan pp;
+  std::string err;
+  if (!analyse_pair(la, T.dims, {}, {}, lc, ctx->precision, pp, err))
+    return fail(ctx, PQ_ERR_INVALID, "decompose_tensor: " + err);
+  // scratch: [A | W | V | sig | order | sweeps], each piece 16-byte aligned
+  auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  const size_t b_mat = up16((size_t)(m * n) * csz), b_v = up16((size_t)(Cn * Cn) * csz),
+               b_sig = up16((size_t)Cn * rsz), b_ord = up16((size_t)Cn * sizeof(int) + sizeof(int));
+  const size_t scratch = 2 * b_mat + b_v + b_sig + b_ord;
+  char* d = nullptr;
+  int st = dev_alloc(ctx, scratch, (void**)&d);
+  if (st) return st;
+  void* A = d;
+  void* W = d + b_mat;
+  void* V = d + 2 * b_mat;
+  void* sig = d + 2 * b_mat + b_v;
+  int* order = (int*)(d + 2 * b_mat + b_v + b_sig);
+  int* sweeps = order + Cn;
+  cudaError_t e = launch_permute(T.dtype, wt, T.ptr, 0, A, pp.g, ctx->stream);
+  ctx->launches += 1;
+  if (e == cudaSuccess) {
+    e = launch_jacobi_svd(wt, A, m, n, W, V, sig, 60, wt == PQ_C128 ? 1e-14 : 1e-6, sweeps, ctx->stream);
+    ctx->launches += 1;
+  }
+  std::vector<double> hs((size_t)Cn);
+  std::vector<float> hsf(wt == PQ_C128 ? 0 : (size_t)Cn);
+  if (e == cudaSuccess && Cn)
+    e = cudaMemcpyAsync(wt == PQ_C128 ? (void*)hs.data() : (void*)hsf.data(), sig, (size_t)Cn * rsz,
+                        cudaMemcpyDeviceToHost, ctx->stream);
+  int h_sweeps = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&h_sweeps, sweeps, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) {
+    dev_free(ctx, d, scratch);
+    return cuda_fail(ctx, e, "decompose_tensor: device SVD");
+  }
+  st = check_status(ctx);
+  if (st) {
+    dev_free(ctx, d, scratch);
+    return st;
+  }
+  for (size_t i = 0; i < hsf.size(); ++i) hs[i] = hsf[i];
+  // the reference's truncation (src/layer1.jl:166-176): singular values above
+  // max(threshold, sqrt(eps)) of their 2-norm, at most max_rank of them
+  std::vector<int> idx((size_t)Cn);
+  for (int i = 0; i < (int)Cn; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return hs[a] > hs[b]; });
+  // eps of the element type (complex128 contexts: FP64; the mixed ones:
+  // FP32, as the reference's ComplexF32 default)
+  const double eps = ctx->precision == PQ_PREC_C128 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+  const double thr = std::max(threshold, std::sqrt(eps));
+  double norm2 = 0.0;
+  for (double v : hs) norm2 += v * v;
+  const double norm = std::sqrt(norm2);
+  int chi = 0;
+  if (norm > 0)
+    for (int i = 0; i < (int)Cn; ++i)
+      if (hs[idx[i]] / norm > thr) ++chi;
+  if (max_rank > 0) chi = std::min(chi, max_rank);
+  std::vector<int64_t> bdims = ld, cdims = {chi};
+  bdims.push_back(chi);
+  cdims.insert(cdims.end(), rd.begin(), rd.end());
+  Tensor Bt, Ct;
+  st = alloc_tensor(ctx, bdims, storage_dtype(ctx, m * chi), Bt);
+  if (!st) {
+    st = alloc_tensor(ctx, cdims, storage_dtype(ctx, n * chi), Ct);
+    if (st) free_tensor(ctx, Bt);
+  }
+  if (!st) {
+    if (chi > 0)
+      e = cudaMemcpyAsync(order, idx.data(), (size_t)chi * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+      e = launch_svd_factors(wt, W, V, sig, order, chi, m, n, Bt.dtype, Bt.ptr, Ct.dtype, Ct.ptr, ctx->stream);
+    ctx->launches += 1;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // idx (host) is read by the copy above
+    if (e != cudaSuccess) {
+      free_tensor(ctx, Bt);
+      free_tensor(ctx, Ct);
+      st = cuda_fail(ctx, e, "decompose_tensor: factors");
+    }
+  }
+  dev_free(ctx, d, scratch);
+  if (st) return st;
+  auto old = ctx->tensors.find(id);
+  free_tensor(ctx, old->second);
+  ctx->tensors.erase(old);
+  put_entry(ctx, left_id, std::move(Bt));
+  put_entry(ctx, right_id, std::move(Ct));
+  *chi_out = chi;
+  if (sweeps_out) *sweeps_out = h_sweeps;
   return PQ_OK;
 }
 

@@ -220,6 +220,18 @@ size_t oz_scratch_bytes(int slices, const GemmDesc& d);
 cudaError_t launch_oz(int slices, int ta, int tb, int tc, const void* A, const void* B, void* C, const GemmDesc& d,
                       void* scratch, size_t scratch_bytes, int* status, cudaStream_t stream);
 
+// Device SVD for bond splits (pq_svd.cu): one-sided Jacobi on A (m x n,
+// column-major, element type wt: PQ_C64 -> complex FP32 arithmetic, PQ_C128
+// -> complex FP64), through W = A (m >= n) or W = A^H (m < n), R x Cn with
+// R = max(m, n), Cn = min(m, n).  Writes W (R x Cn) and V (Cn x Cn) of type
+// wt and sig[Cn] (float or double, unsorted column norms).
+cudaError_t launch_jacobi_svd(int wt, const void* A, int64_t m, int64_t n, void* W, void* V, void* sig,
+                              int max_sweeps, double tol, int* sweeps, cudaStream_t s);
+// B (m x chi) = U sqrt(S) and C (chi x n) = sqrt(S) V^H of the chi singular
+// values order[0..chi) (columns of W), stored as tb / tc.
+cudaError_t launch_svd_factors(int wt, const void* W, const void* V, const void* sig, const int* order, int chi,
+                               int64_t m, int64_t n, int tb, void* B, int tc, void* Cm, cudaStream_t s);
+
 }  // namespace pq
 
 struct pq_ctx {

@@ -5,8 +5,9 @@ Same order of operations as the reference: gate nodes are absorbed into the
 per-qubit MPS tensors layer by layer (``contract_pair``, one device kernel per
 pair), then the bonds between neighbouring updated tensors are compressed by
 a contraction followed by an SVD split with a relative threshold and a
-maximum rank.  The SVD itself runs in the backend's ``decompose_tensor`` (on
-the host in FP64 for the GB300 backend; a batched device SVD is not built).
+maximum rank.  The SVD itself runs in the backend's ``decompose_tensor``:
+for the GB300 backend LAPACK on the host (the default) or the library's
+one-sided Jacobi SVD on the device (``GB300Backend(svd="device")``).
 """
 from __future__ import annotations
 

@@ -529,3 +529,10 @@ def test_autotune_plan_pairs_and_names(pq):
     assert AT.plan_pairs(Hyper) == [([0, 1], [2, 3], [1], [3])]
     assert AT.choice_name((2, 64, 2)) == "tcgen05/tn64/swapped" and AT.choice_name((4, 0, 0)) == "skinny"
     assert len(AT.source_hash()) == 16
+
+
+def test_backend_rejects_unknown_svd_mode(pq):
+    """The bond-split location is "host" or "device"; anything else is
+    refused before the library is touched."""
+    with pytest.raises(ValueError):
+        pq.GB300Backend(pq.PREC_C64, svd="gpu")
