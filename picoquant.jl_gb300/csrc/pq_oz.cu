@@ -312,15 +312,23 @@ __device__ __forceinline__ float2 inv_scale(int e) {
 __device__ __forceinline__ float scale_row(float x, int, float2 f) { return (x * f.x) * f.y; }
 __device__ __forceinline__ double scale_row(double x, int e, float2) { return ldexp(x, -e); }
 
+// One plane tile (ROWS x 16) is shared by PARTS blocks (blockIdx.x = kt PARTS
+// + part), each slicing TILE / PARTS values: complex128 B is sliced in FP64,
+// whose GB300 rate is low, so the work is spread over many SMs.
+template <typename T, int ROWS, int NSL>
+__host__ __device__ constexpr int pack_parts() {
+  return ROWS * TK / 256 > 0 ? ROWS * TK / 256 : 1;
+}
 template <typename T, int ROWS, int NSL>
 __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_bfloat16* __restrict__ planes,
                                                  const __grid_constant__ GemmDesc d, int side, int64_t rows,
                                                  int64_t rtiles, int64_t ktiles, const int* __restrict__ e_in) {
-  constexpr int TILE = ROWS * TK, GROUPS = ROWS / 8;
+  constexpr int TILE = ROWS * TK, GROUPS = ROWS / 8, PARTS = pack_parts<T, ROWS, NSL>(), PER = TILE / PARTS;
   __shared__ int64_t roff[ROWS];
   __shared__ int rexp[ROWS];
   __shared__ int64_t koff[TK];
-  const int64_t kt = blockIdx.x, rt = blockIdx.y, z = blockIdx.z;
+  const int64_t kt = blockIdx.x / PARTS, rt = blockIdx.y, z = blockIdx.z;
+  const int part = (int)(blockIdx.x % PARTS);
   const int nrm = side == 0 ? d.nm : d.nn;
   const int64_t* rdim = side == 0 ? d.mdim : d.ndim;
   const int64_t* rstr = side == 0 ? d.msa : d.nsb;
@@ -340,7 +348,7 @@ __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_b
   const int64_t zo = decode(z, d.nz, d.zdim, zstr);
   using R = typename Real<T>::R;
   __nv_bfloat16* tile = planes + (((z * rtiles + rt) * ktiles + kt) * Sl<NSL>::planes) * (int64_t)TILE;
-  for (int o = threadIdx.x; o < TILE; o += blockDim.x) {
+  for (int o = part * PER + threadIdx.x; o < (part + 1) * PER; o += blockDim.x) {
     // o = ((kc * GROUPS + g) * 8 + r8) * 8 + k8: core matrix (kc, g), row r8, K k8
     const int core = o >> 6, within = o & 63;
     const int kc = core / GROUPS, g = core - kc * GROUPS;
@@ -835,12 +843,15 @@ bool needs_swap(const GemmDesc& d) {
   return d.M < 64 && d.N > d.M;
 }
 
+// B's column exponents (16 columns per block, 16 threads on each: B is the
+// small side, so its pass needs many blocks to be short), then its slices.
 template <typename T, int ROWS, int NSL>
 void prep_b(const void* X, __nv_bfloat16* planes, int* e, const GemmDesc& d, int64_t rtiles, int64_t kt,
             cudaStream_t s) {
-  k_oz_exp<T, ROWS><<<dim3((unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, d, 1, d.N, e);
-  k_oz_pack<T, ROWS, NSL><<<dim3((unsigned)kt, (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>((const T*)X, planes, d, 1,
-                                                                                       d.N, rtiles, kt, e);
+  k_oz_exp<T, 16><<<dim3((unsigned)ceil_div(d.N, 16), (unsigned)d.Z), 256, 0, s>>>((const T*)X, d, 1, d.N, e);
+  constexpr int parts = pack_parts<T, ROWS, NSL>();
+  k_oz_pack<T, ROWS, NSL><<<dim3((unsigned)(kt * parts), (unsigned)rtiles, (unsigned)d.Z), 256, 0, s>>>(
+      (const T*)X, planes, d, 1, d.N, rtiles, kt, e);
 }
 
 template <typename T, int NSL>
