@@ -235,11 +235,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="grid6x6_d16_sliced",
                     choices=["grid6x6_d16_sliced", "grid6x6_d16_accuracy", "grid4x5_d12_amps", "grid7x7_d14_learned",
-                             "uneven512", "pair"],
+                             "uneven512", "pair", "svd"],
                     help="grid7x7_d14_learned: learned plan selection over sweep orders and 256 seeded greedy "
                          "orders for a 7x7 depth-14 single amplitude, end to end; pair: one pairwise contraction "
                          "of the dominant shape (M x K c64 boundary times K x N c128 gate-column tensor), for "
-                         "kernel profiling")
+                         "kernel profiling; svd: bond splits (decompose_tensor) on the host and on the device")
     ap.add_argument("--candidates", type=int, default=256, help="seeded random-greedy orders ranked by the model")
     ap.add_argument("--circuits", type=int, default=512, help="circuits of the uneven512 workload")
     ap.add_argument("--amplitudes", type=int, default=8, help="amplitudes of the grid6x6_d16_accuracy workload")
@@ -247,6 +247,8 @@ def main():
     ap.add_argument("--sv-budget-gb", type=float, default=64.0,
                     help="uneven512: state bytes resident at once in the grouped state-vector batch")
     ap.add_argument("--pair", default="1048576x256x256", help="M x N x K of the pair workload")
+    ap.add_argument("--svd-sizes", default="16x16,64x64,128x128,256x256,1024x64",
+                    help="m x n matrix sizes of the svd workload")
     ap.add_argument("--pair-order", default="mk", choices=["mk", "km"],
                     help="memory order of the pair's A: contiguous along M (mk) or along K (km)")
     ap.add_argument("--rows", type=int, default=6, help="grid rows of the sliced workload (smaller for ncu)")
@@ -286,7 +288,52 @@ def main():
         return run_uneven(args)
     if args.workload == "grid6x6_d16_accuracy":
         return run_accuracy(args)
+    if args.workload == "svd":
+        return run_svd(args)
     return run_gb300(args, world, rank)
+
+
+def run_svd(args):
+    """Bond splits (decompose_tensor!, src/layer1.jl:146-184) of random
+    complex m x n tensors: per size and context precision, the time of one
+    split on the host (download, LAPACK in FP64, upload) and on the device
+    (pq_decompose_tensor, one-sided Jacobi), the median of --steps timed
+    splits after --warmup, with the device's sweep count and the largest
+    difference of the singular values (squared column norms of the left
+    factor) between the two, relative to the largest."""
+    import time
+
+    import __graft_entry__ as g
+
+    pq = g.load_package()
+    rng = np.random.default_rng(0)
+    for prec_name, prec in (("c64", pq.PREC_C64), ("c128", pq.PREC_C128)):
+        for size in args.svd_sizes.split(","):
+            m, n = (int(x) for x in size.lower().split("x"))
+            T = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+            rec = {"workload": "svd", "precision": prec_name, "m": m, "n": n}
+            sig = {}
+            for mode in ("host", "device"):
+                be = pq.GB300Backend(prec, svd=mode)
+                ts = []
+                for it in range(args.warmup + args.steps):
+                    be.save_tensor_data("t", T)
+                    be.sync()
+                    t0 = time.perf_counter()
+                    chi = be.decompose_tensor("t", [1], [2], left_label="b", right_label="c")
+                    be.sync()
+                    if it >= args.warmup:
+                        ts.append(time.perf_counter() - t0)
+                B = np.asarray(be.load_tensor_data("b")).reshape(m, chi, order="F")
+                sig[mode] = np.sum(np.abs(B) ** 2, axis=0)
+                rec[f"{mode}_ms"] = float(np.median(ts)) * 1e3
+                rec["chi"] = chi
+                if mode == "device":
+                    rec["sweeps"] = be.last_svd_sweeps
+                be.close()
+            rec["sigma_rel_diff"] = float(np.max(np.abs(sig["host"] - sig["device"])) / np.max(sig["host"]))
+            print(json.dumps(rec), flush=True)
+    return 0
 
 
 def run_accuracy(args):

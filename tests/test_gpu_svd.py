@@ -115,6 +115,9 @@ def test_device_svd_truncates_like_the_reference(pq):
     chi, B, Cm = _split(pq, be, T, [1, 2], [3], threshold=1e-4)
     assert chi == 4
     _check(pq, T, [1, 2], [3], B, Cm, chi, 1e-12, threshold=1e-4)
+    # an all-zero tensor has no singular value above the threshold: chi = 0
+    chi, B, Cm = _split(pq, be, np.zeros((4, 2, 8), dtype=np.complex128), [1, 2], [3])
+    assert chi == 0 and B.shape == (4, 2, 0) and Cm.shape == (0, 8)
     be.close()
 
 
