@@ -67,12 +67,19 @@ bool groupable(const Step& s) {
          s.tc == PQ_C128 && s.pp.csize >= 1 && s.pp.csize <= kGroupSmall && s.pp.g.ksize <= kGroupK;
 }
 
-// Launch groups: every maximal run of consecutive small steps (same batched
-// flag) is reordered by dependency level within the run -- a step's level is
-// one more than the highest level of a producer inside the run -- and each
-// level becomes one launch of up to kGroupMax steps (the per-qubit chains of
-// a circuit advance together).  Steps outside runs keep their positions, so
-// every step still follows its producers.
+// Launch groups of small steps, in two parts.
+//  1. Hoisted: every small step whose producers are leaves or hoisted small
+//     steps (the per-qubit chains of small gate tensors that do not wait for
+//     any large intermediate).  These run first, by dependency level -- one
+//     more than the highest level of a hoisted producer -- and each (level,
+//     batched flag) becomes launches of up to kGroupMax steps, so the chains
+//     of the whole plan advance together.
+//  2. The rest keep their order; within every maximal run of consecutive small
+//     steps (same batched flag) the steps are reordered by dependency level
+//     inside the run and each level becomes one launch of up to kGroupMax.
+// Every step still follows its producers, and the batched (per slice batch)
+// and unbatched (once per call) steps keep their relative orders, so both the
+// plain and the sliced executors stay valid.
 void form_groups(Compiled& cp) {
   const int n = (int)cp.steps.size();
   std::vector<int> prod(cp.labels.size(), -1);
@@ -82,39 +89,88 @@ void form_groups(Compiled& cp) {
   steps.reserve(n);
   order.reserve(n);
   int gid = 0;
-  for (int i = 0; i < n;) {
-    if (!groupable(cp.steps[i])) {
-      steps.push_back(cp.steps[i]);
-      order.push_back(cp.order[i]);
+  // emit the steps idx[a..b) (original positions) as one launch group when
+  // there are at least two of them
+  auto emit = [&](const std::vector<int>& idx, size_t a, size_t b) {
+    const bool grp = b - a >= 2;
+    for (size_t c = a; c < b; ++c) {
+      Step st = cp.steps[idx[c]];
+      st.group = grp ? gid : -1;
+      steps.push_back(st);
+      order.push_back(cp.order[idx[c]]);
+    }
+    if (grp) ++gid;
+  };
+  // 1. hoisted small steps
+  std::vector<char> hoisted(n, 0);
+  std::vector<int> hlevel(n, 0);
+  for (int i = 0; i < n; ++i) {
+    if (!groupable(cp.steps[i])) continue;
+    bool ok = true;
+    int L = 0;
+    for (int v : {cp.steps[i].x, cp.steps[i].y}) {
+      if (v < 0 || v < cp.nleaves) continue;
+      const int pi = prod[v];
+      if (pi < 0 || !hoisted[pi]) {
+        ok = false;
+        break;
+      }
+      L = std::max(L, hlevel[pi] + 1);
+    }
+    hoisted[i] = ok;
+    hlevel[i] = L;
+  }
+  std::vector<int> hidx;
+  for (int i = 0; i < n; ++i)
+    if (hoisted[i]) hidx.push_back(i);
+  std::stable_sort(hidx.begin(), hidx.end(), [&](int a, int b) {
+    if (hlevel[a] != hlevel[b]) return hlevel[a] < hlevel[b];
+    return (int)cp.steps[a].batched < (int)cp.steps[b].batched;
+  });
+  for (size_t a = 0; a < hidx.size();) {
+    size_t b = a;
+    while (b < hidx.size() && hlevel[hidx[b]] == hlevel[hidx[a]] &&
+           cp.steps[hidx[b]].batched == cp.steps[hidx[a]].batched && b - a < (size_t)kGroupMax)
+      ++b;
+    emit(hidx, a, b);
+    a = b;
+  }
+  // 2. the rest, runs of consecutive small steps grouped by level
+  std::vector<int> rest;
+  for (int i = 0; i < n; ++i)
+    if (!hoisted[i]) rest.push_back(i);
+  const int nr = (int)rest.size();
+  std::vector<int> rpos(n, -1);
+  for (int q = 0; q < nr; ++q) rpos[rest[q]] = q;
+  for (int i = 0; i < nr;) {
+    const Step& si = cp.steps[rest[i]];
+    if (!groupable(si)) {
+      emit(rest, i, i + 1);
       ++i;
       continue;
     }
     int j = i;
-    while (j < n && groupable(cp.steps[j]) && cp.steps[j].batched == cp.steps[i].batched) ++j;
+    while (j < nr && groupable(cp.steps[rest[j]]) && cp.steps[rest[j]].batched == si.batched) ++j;
     std::vector<int> lvl(j - i, 0);
     for (int t = i; t < j; ++t) {
       int L = 0;
-      for (int v : {cp.steps[t].x, cp.steps[t].y}) {
-        if (v < 0) continue;
+      for (int v : {cp.steps[rest[t]].x, cp.steps[rest[t]].y}) {
+        if (v < 0 || v < cp.nleaves) continue;
         const int pi = prod[v];
-        if (pi >= i && pi < t) L = std::max(L, lvl[pi - i] + 1);
+        const int q = pi >= 0 ? rpos[pi] : -1;
+        if (q >= i && q < t) L = std::max(L, lvl[q - i] + 1);
       }
       lvl[t - i] = L;
     }
     std::vector<int> idx(j - i);
     for (int t = 0; t < j - i; ++t) idx[t] = t;
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return lvl[a] < lvl[b]; });
-    for (size_t a = 0; a < idx.size();) {
+    std::vector<int> run(j - i);
+    for (int t = 0; t < j - i; ++t) run[t] = rest[i + idx[t]];
+    for (size_t a = 0; a < run.size();) {
       size_t b = a;
-      while (b < idx.size() && lvl[idx[b]] == lvl[idx[a]] && b - a < (size_t)kGroupMax) ++b;
-      const bool grp = b - a >= 2;
-      for (size_t c = a; c < b; ++c) {
-        Step st = cp.steps[i + idx[c]];
-        st.group = grp ? gid : -1;
-        steps.push_back(st);
-        order.push_back(cp.order[i + idx[c]]);
-      }
-      if (grp) ++gid;
+      while (b < run.size() && lvl[idx[b]] == lvl[idx[a]] && b - a < (size_t)kGroupMax) ++b;
+      emit(run, a, b);
       a = b;
     }
     i = j;
@@ -133,7 +189,11 @@ void form_groups(Compiled& cp) {
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Liveness-driven first-fit arena assignment.  `pinned[v]` values are never
-// released once computed (used for sliced execution).
+// released once computed (used for sliced execution: values computed once and
+// read by the batched steps).  They are also never placed in released space:
+// the sliced executor runs every unbatched step before the batched ones, so a
+// block that a batched value used earlier in the step order is written again
+// by the batched pass after the pinned value was stored there.
 void assign_arena(Compiled& cp, const std::vector<char>& pinned) {
   const int nv = (int)cp.labels.size();
   std::vector<int> last_use(nv, -1);
@@ -183,7 +243,12 @@ void assign_arena(Compiled& cp, const std::vector<char>& pinned) {
       Step& s = cp.steps[t];
       const int r = cp.nleaves + cp.order[t];
       const size_t sz = align_up(std::max<size_t>(s.bytes, 16), 256);
-      s.off = take(sz);
+      if (pinned[r]) {
+        s.off = top;
+        top += sz;
+      } else {
+        s.off = take(sz);
+      }
       voff[r] = s.off;
       vsz[r] = sz;
     }
