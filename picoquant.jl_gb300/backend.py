@@ -174,6 +174,36 @@ class GB300Backend:
                                       L.arr(C.c_int64, dims or [0]), ptrs, L.arr(C.c_int32, dts))
         self._check(rc, "save_tensors")
 
+    def prepare_tensors(self, items):
+        """The argument arrays of ``save_tensors`` for a fixed list of (label,
+        host array) pairs, built once, for a caller that uploads the same
+        tensors again and again (new values written into the same arrays,
+        e.g. the gates of a parameterised circuit before every contraction).
+        Every array must be Fortran-ordered complex64 or complex128 and stay
+        alive, with its shape, while the result is in use; ``save_prepared``
+        then uploads the arrays' current contents with one library call."""
+        items = list(items)
+        ids, ranks, dims, dts, keep = [], [], [], [], []
+        for label, a in items:
+            if not isinstance(a, np.ndarray) or a.dtype not in (np.complex64, np.complex128) or not (
+                    a.flags.f_contiguous or a.ndim <= 1):
+                raise ValueError(f"prepare_tensors({label}): needs a Fortran-ordered complex64/complex128 array")
+            keep.append(a)
+            ids.append(self.id_of(label))
+            ranks.append(a.ndim)
+            dims.extend(a.shape)
+            dts.append(L.PQ_C64 if a.dtype == np.complex64 else L.PQ_C128)
+        n = len(keep)
+        return (n, L.arr(C.c_int64, ids or [0]), L.arr(C.c_int32, ranks or [0]), L.arr(C.c_int64, dims or [0]),
+                (C.c_void_p * max(1, n))(*[a.ctypes.data for a in keep]), L.arr(C.c_int32, dts or [0]), keep)
+
+    def save_prepared(self, prepared):
+        """Upload the current contents of the arrays of ``prepare_tensors``
+        (``pq_save_tensors``: one staging copy and one device scatter)."""
+        n, ids, ranks, dims, ptrs, dts, _ = prepared
+        if n:
+            self._check(self.lib.pq_save_tensors(self.ctx, n, ids, ranks, dims, ptrs, dts), "save_tensors")
+
     def has_tensor(self, label) -> bool:
         key = str(label)
         return key in self._ids and bool(self.lib.pq_has_tensor(self.ctx, self._ids[key]))

@@ -45,3 +45,25 @@ def test_save_tensors_feeds_a_plan(pq, O):
         assert np.max(np.abs(out - O.statevector(6, gates))) < 1e-12
     plan.close()
     be.close()
+
+
+def test_prepared_uploads_follow_the_arrays(pq):
+    """prepare_tensors builds the argument arrays once; save_prepared uploads
+    whatever the host arrays hold at that moment (values rewritten in place
+    between uploads), and refuses arrays it cannot upload without a copy."""
+    rng = np.random.default_rng(3)
+    arrs = [np.asfortranarray(rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(dt)
+            for s, dt in (((2, 2), np.complex128), ((2, 2, 2), np.complex64), ((5,), np.complex128))]
+    be = pq.GB300Backend(pq.PREC_C64)
+    prep = be.prepare_tensors([(f"p{i}", a) for i, a in enumerate(arrs)])
+    for step in range(3):
+        for a in arrs:
+            a[...] = (step + 1) * (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape))
+        be.save_prepared(prep)
+        for i, a in enumerate(arrs):
+            np.testing.assert_array_equal(be.load_tensor_data(f"p{i}"), a.astype(np.complex128))
+    with pytest.raises(ValueError):
+        be.prepare_tensors([("c", np.ones((3, 4), np.complex128))])  # C-ordered
+    with pytest.raises(ValueError):
+        be.prepare_tensors([("r", np.ones((2, 2)))])  # real
+    be.close()
