@@ -111,13 +111,47 @@ struct OzCfg {
   static constexpr uint32_t b_bytes = Sl<NSL>::planes * kBTile * 2;        // B planes of one K tile
   static constexpr uint32_t stage_bytes = NSL * kStackBytes + b_bytes;
   static constexpr int stages = (TN == 128 && NSL >= 4) ? 3 : 4;
-  // accumulator sets (three levels of TN columns each): two for TN <= 64, so
-  // that the MMAs of the next tile run while the epilogue drains this one
+  // 16-wide tiles: one MMA per A slice i against B slices 0 .. NSL-1-i side
+  // by side (N = 16 (NSL - i)), every slice pair in its own TMEM region
+  static constexpr bool narrow = TN == 16;
+  // accumulator columns of one tile: three levels of TN columns, or the
+  // NSL (NSL + 1) / 2 pair regions of 16 columns
+  static constexpr int set_cols = narrow ? 8 * NSL * (NSL + 1) : 3 * TN;
+  // accumulator sets: two for TN <= 64, so that the MMAs of the next tile
+  // run while the epilogue drains this one
   static constexpr int acc_sets = TN <= 64 ? 2 : 1;
-  static constexpr uint32_t tmem_cols = TN == 128 ? 512 : (TN == 64 ? 512 : (TN == 32 ? 256 : 128));
+  static constexpr uint32_t tmem_cols =
+      TN == 128 ? 512 : (TN == 64 ? 512 : (TN == 32 ? 256 : (2 * set_cols > 256 ? 512 : 256)));
   static constexpr int cw = TN / 2;                                         // columns per epilogue warp
-  static_assert(acc_sets * 3 * TN <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
+  static_assert(acc_sets * set_cols <= (int)tmem_cols && cw % 8 == 0 && stage_bytes % 1024 == 0, "tile width");
 };
+
+// First TMEM column of A slice i's region in a narrow tile: the regions of
+// slices 0 .. i-1 hold NSL, NSL - 1, ... pair blocks of 16 columns.
+template <int NSL>
+__host__ __device__ constexpr int narrow_col(int i) {
+  return 16 * (i * NSL - i * (i - 1) / 2);
+}
+// The slice pairs of level >= 2, smallest level first: the p-th is
+// (rest_i, rest_level - rest_i); level l holds the l + 1 pairs i = 0 .. l.
+template <int NSL>
+__host__ __device__ constexpr int rest_level(int p) {
+  int l = NSL - 1;
+  while (p > l) {
+    p -= l + 1;
+    --l;
+  }
+  return l;
+}
+template <int NSL>
+__host__ __device__ constexpr int rest_i(int p) {
+  int l = NSL - 1;
+  while (p > l) {
+    p -= l + 1;
+    --l;
+  }
+  return p;
+}
 
 // slice pairs, level 0 first, then level 1, then the higher levels (the
 // inexact accumulator takes its small terms first).  Five slices:
@@ -361,10 +395,23 @@ __global__ void __launch_bounds__(256) k_oz_pack(const T* __restrict__ X, __nv_b
       slices<R, NSL>(scale2((R)v.x, -rexp[r]), re);
       slices<R, NSL>(scale2((R)v.y, -rexp[r]), im);
     }
+    if constexpr (ROWS == 16) {
+      // 16-wide tiles: per part (Re, Im) one block of the NSL slices side by
+      // side along N (slice i = rows 16 i .. 16 i + 15, row groups 2 i and
+      // 2 i + 1), so that slices 0 .. m form one operand of 16 (m + 1) rows
+      const int r8 = within >> 3, k8 = within & 7;
 #pragma unroll
-    for (int i = 0; i < NSL; ++i) {
-      tile[(0 * NSL + i) * TILE + o] = __float2bfloat16_rn(re[i]);
-      tile[(1 * NSL + i) * TILE + o] = __float2bfloat16_rn(im[i]);
+      for (int i = 0; i < NSL; ++i) {
+        const int q = ((kc * (NSL * GROUPS) + i * GROUPS + g) * 8 + r8) * 8 + k8;
+        tile[0 * NSL * TILE + q] = __float2bfloat16_rn(re[i]);
+        tile[1 * NSL * TILE + q] = __float2bfloat16_rn(im[i]);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NSL; ++i) {
+        tile[(0 * NSL + i) * TILE + o] = __float2bfloat16_rn(re[i]);
+        tile[(1 * NSL + i) * TILE + o] = __float2bfloat16_rn(im[i]);
+      }
     }
   }
 }
@@ -512,6 +559,22 @@ __global__ void __launch_bounds__(kThreads, 1)
           fence_after();
           const uint32_t sa = smem_u32(sm.stage[s]);
           const uint64_t a0 = smem_desc(sa, ALBO, SBO);
+          if constexpr (CF::narrow) {
+            // B block per part: NSL slices x 2 row groups per K half
+            const uint64_t bn = smem_desc(sa + kSlices * kStackBytes, NSL * 2 * 128, SBO);
+#pragma unroll
+            for (int i = 0; i < NSL; ++i) {
+              const uint32_t dl = tmem + (uint32_t)(b * CF::set_cols + narrow_col<NSL>(i));
+              const uint64_t x1 = a0 + (uint64_t)((i * kStackBytes) >> 4);            // [Ar; Ai]
+              const uint64_t x2 = a0 + (uint64_t)((i * kStackBytes + 8 * 128) >> 4);  // [Ai; -Ar]
+              const uint64_t bi = bn + (uint64_t)((NSL * CF::kBTile * 2) >> 4);       // the Im block
+              const uint32_t acc = kt == 0 ? 0u : 1u;
+              mma_bf16(dl, x1, bn, idesc_bf16(128, 16 * (NSL - i)), acc);   // [Ar.Br ; Ai.Br], slices 0..NSL-1-i
+              mma_bf16(dl, x2, bi, idesc_bf16(128, 16 * (NSL - i), true), 1u);
+            }
+            mma_commit(&sm.empty[s]);
+            continue;
+          }
           const uint64_t b0 = smem_desc(sa + kSlices * kStackBytes, BLBO, SBO);
 #pragma unroll
           for (int p = 0; p < kPairs; ++p) {
@@ -746,7 +809,40 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();  // the TMEM loads are warp-collective
         const uint32_t col = (uint32_t)(b * 3 * TN + h * CW + piece * PW);
         float l0[PW], l1[PW], l2[PW];
-        if constexpr (PW == 16) {
+        if constexpr (CF::narrow) {
+          // the slice-pair regions (each an exact sum over K): level 0 =
+          // (0,0); level 1 = (0,1) + (1,0), exact; levels 2 .. NSL-1 summed
+          // in FP32, the smallest first, four regions per TMEM wait
+          static_assert(PW == 8, "narrow tiles: 8 columns per epilogue warp");
+          const uint32_t rb = lane_base + (uint32_t)(b * CF::set_cols + h * CW + piece * PW);
+          float t0[PW], t1[PW];
+          tmem_ld8(rb + narrow_col<NSL>(0), l0);
+          tmem_ld8(rb + narrow_col<NSL>(0) + 16, t0);
+          tmem_ld8(rb + narrow_col<NSL>(1), t1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int q = 0; q < PW; ++q) {
+            l1[q] = t0[q] + t1[q];
+            l2[q] = 0.f;
+          }
+          constexpr int NR = NSL * (NSL + 1) / 2 - 3;
+#pragma unroll
+          for (int p0 = 0; p0 < NR; p0 += 4) {
+            float tb[4][PW];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (p0 + u < NR)
+                tmem_ld8(rb + narrow_col<NSL>(rest_i<NSL>(p0 + u)) +
+                             16 * (rest_level<NSL>(p0 + u) - rest_i<NSL>(p0 + u)),
+                         tb[u]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (p0 + u < NR)
+#pragma unroll
+                for (int q = 0; q < PW; ++q) l2[q] += tb[u][q];
+          }
+        } else if constexpr (PW == 16) {
           tmem_ld16(lane_base + col + 0 * TN, l0);
           tmem_ld16(lane_base + col + 1 * TN, l1);
           tmem_ld16(lane_base + col + 2 * TN, l2);
