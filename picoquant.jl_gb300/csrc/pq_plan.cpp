@@ -58,13 +58,15 @@ struct Compiled {
   std::vector<int> gdesc_of;       // per step: index into gdesc, or -1
 };
 
-// Small steps: complex128 generic contractions of at most kGroupSmall result
-// elements and K <= kGroupK.  They are launch-bound one by one.
+// Small steps: complex128 generic or skinny contractions of at most
+// kGroupSmall result elements and K <= kGroupK.  They are launch-bound one by
+// one; in a group they run as generic contractions side by side.
 constexpr int64_t kGroupSmall = 1 << 16;
 
 bool groupable(const Step& s) {
-  return !s.is_copy && s.y >= 0 && s.pp.kclass == KC_GENERIC && s.ta == PQ_C128 && s.tb == PQ_C128 &&
-         s.tc == PQ_C128 && s.pp.csize >= 1 && s.pp.csize <= kGroupSmall && s.pp.g.ksize <= kGroupK;
+  return !s.is_copy && s.y >= 0 && (s.pp.kclass == KC_GENERIC || s.pp.kclass == KC_SKINNY) &&
+         s.ta == PQ_C128 && s.tb == PQ_C128 && s.tc == PQ_C128 && s.pp.csize >= 1 && s.pp.csize <= kGroupSmall &&
+         s.pp.g.ksize <= kGroupK;
 }
 
 // Launch groups of small steps, in two parts.
