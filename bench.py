@@ -1139,6 +1139,11 @@ def report(args, pq, w, be, plan, rows, cols, depth, value, t_total, times, laun
                                                      prec_name, ms_step)
         extra["kernel_classes"] = kinfo
         extra["roofline_all_steps"] = overall
+        # the fidelity check: the open-output result is the whole 2^20 state,
+        # whose squared norm (FP64, on the device) is 1 for a unitary circuit
+        n2 = be.norm2(w["plan"].execute())
+        extra["state_fidelity_check"] = {"norm2": n2, "abs_norm2_minus_1": abs(n2 - 1.0),
+                                         "how": "pq_tensor_norm2: FP64 compensated sum of |psi|^2 on the device"}
         v, desc = _cpu_sample_amps(O, rows, cols, depth)
         cpu = {"value": v, "unit": "amplitudes/s", "cores": host_threads(), "kind": "port", "sample": desc}
     line = {

@@ -140,6 +140,13 @@ int pq_tensor_shape(pq_ctx* ctx, int64_t id, int* rank, int64_t* dims);
 int pq_has_tensor(pq_ctx* ctx, int64_t id);
 /* src/backends/interactive.jl:159-161 `delete_tensor!`. */
 int pq_delete_tensor(pq_ctx* ctx, int64_t id);
+/* Squared 2-norm of tensor `id`, sum |x|^2 over its elements, accumulated in
+ * FP64 with compensated (Neumaier) sums on the device, in a fixed order
+ * (deterministic), written to *norm2.  The fidelity check of a state vector:
+ * a unitary circuit's output has norm2 = 1, so |norm2 - 1| measures the
+ * accumulated error.  No counterpart in the reference, which would take
+ * LinearAlgebra.norm of the downloaded array.  Synchronises. */
+int pq_tensor_norm2(pq_ctx* ctx, int64_t id, double* norm2);
 /* src/backends/interactive.jl:84-88 `save_output(backend, node, name)`:
  * the tensor `node` is also stored under `name` (a copy on the device). */
 int pq_save_output(pq_ctx* ctx, int64_t node, int64_t name);

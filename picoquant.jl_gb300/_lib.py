@@ -79,6 +79,7 @@ SIGNATURES = [
     ("pq_permute_tensor", C.c_int, [vp, C.c_int64, i32p, C.c_int]),
     ("pq_reshape_tensor", C.c_int, [vp, C.c_int64, C.c_int, i32p, i32p]),
     ("pq_view_tensor", C.c_int, [vp, C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64]),
+    ("pq_tensor_norm2", C.c_int, [vp, C.c_int64, C.POINTER(C.c_double)]),
     ("pq_decompose_tensor", C.c_int, [vp, C.c_int64, C.c_int, i32p, C.c_int, i32p, C.c_double, C.c_int, C.c_int64,
                                       C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("pq_gather_elements", C.c_int, [vp, C.c_int64, i64p, C.c_int64, vp, C.c_int]),

@@ -204,6 +204,13 @@ class GB300Backend:
         if n:
             self._check(self.lib.pq_save_tensors(self.ctx, n, ids, ranks, dims, ptrs, dts), "save_tensors")
 
+    def norm2(self, label) -> float:
+        """Squared 2-norm of a tensor, accumulated in FP64 on the device
+        (``pq_tensor_norm2``): the fidelity check of a state vector."""
+        v = C.c_double(0.0)
+        self._check(self.lib.pq_tensor_norm2(self.ctx, self.id_of(label), C.byref(v)), f"tensor_norm2({label})")
+        return v.value
+
     def has_tensor(self, label) -> bool:
         key = str(label)
         return key in self._ids and bool(self.lib.pq_has_tensor(self.ctx, self._ids[key]))

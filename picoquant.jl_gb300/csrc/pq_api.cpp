@@ -375,6 +375,25 @@ int pq_delete_tensor(pq_ctx* c, int64_t id) {
   return PQ_OK;
 }
 
+int pq_tensor_norm2(pq_ctx* c, int64_t id, double* norm2) {
+  CTX_OR_FAIL(c);
+  if (!norm2) return fail(ctx, PQ_ERR_INVALID, "tensor_norm2: null output");
+  auto it = ctx->tensors.find(id);
+  if (it == ctx->tensors.end()) return fail(ctx, PQ_ERR_NOT_FOUND, "tensor_norm2: no tensor " + std::to_string(id));
+  const Tensor& T = it->second;
+  const int nb = norm2_blocks(T.size);
+  const size_t bytes = (size_t)(2 * nb + 1) * sizeof(double);
+  double* d = nullptr;
+  int st = dev_alloc(ctx, bytes, (void**)&d);
+  if (st) return st;
+  cudaError_t e = launch_norm2(T.dtype, T.ptr, T.size, d, d + 2 * nb, ctx->stream);
+  ctx->launches += 2;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(norm2, d + 2 * nb, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  dev_free(ctx, d, bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor_norm2");
+  return check_status(ctx);  // also completes the copy
+}
+
 int pq_save_output(pq_ctx* c, int64_t node, int64_t name) {
   CTX_OR_FAIL(c);
   auto it = ctx->tensors.find(node);

@@ -203,6 +203,10 @@ cudaError_t launch_slice_gather(int dt, const void* in, void* out, const Generic
                                 int nsl, const int64_t* sl_dim, const int64_t* sl_stride,
                                 int64_t s0, int64_t nb, int64_t s_end, cudaStream_t stream);
 // Neumaier FP64 sum over the batch axis: acc[e] += sum_b X[e + n*b].
+// FP64 squared 2-norm of n complex elements into *out (device); `part`
+// holds 2 * norm2_blocks(n) doubles of scratch.
+int norm2_blocks(int64_t n);
+cudaError_t launch_norm2(int dt, const void* X, int64_t n, double* part, double* out, cudaStream_t stream);
 cudaError_t launch_slice_sum(int dt, const void* X, int64_t n, int64_t nb,
                              double* acc, double* comp, cudaStream_t stream);
 // Split-precision tensor-core GEMM-class contraction (pq_tc.cu).  Returns

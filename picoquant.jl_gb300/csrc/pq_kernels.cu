@@ -6,6 +6,8 @@
 // complex128).  Results stored as complex128 are accumulated in FP64; results
 // stored as complex64 are accumulated in FP32 over chunks of kChunk terms that
 // are folded with Kahan compensation.
+#include <algorithm>
+
 #include "pq_types.cuh"
 
 namespace pq {
@@ -379,6 +381,56 @@ __global__ void k_slice_sum(const T* __restrict__ X, int64_t n, int64_t nb, doub
     acc[2 * e + 1] = i_s;
     comp[2 * e + 1] = i_c;
   }
+}
+
+// Squared 2-norm of a complex tensor in FP64 (the fidelity check of a state
+// vector): pass 1, every thread a Neumaier sum of |x|^2 over a grid-stride
+// range, the block's sums folded by one thread in a fixed order into
+// part[block] (value, compensation); pass 2, one thread folds the blocks' parts
+// in block order.  Deterministic: no atomics.
+constexpr int kNormThreads = 256;
+template <typename T>
+__global__ void __launch_bounds__(kNormThreads) k_norm2(const T* __restrict__ X, int64_t n, double* part) {
+  __shared__ double ss[kNormThreads], sc[kNormThreads];
+  double s = 0, c = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T v = X[i];
+    neumaier(s, c, (double)v.x * (double)v.x);
+    neumaier(s, c, (double)v.y * (double)v.y);
+  }
+  ss[threadIdx.x] = s;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bs = 0, bc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      neumaier(bs, bc, ss[t]);
+      bc += sc[t];
+    }
+    part[2 * blockIdx.x] = bs;
+    part[2 * blockIdx.x + 1] = bc;
+  }
+}
+__global__ void k_norm2_fold(const double* __restrict__ part, int nblocks, double* out) {
+  if (threadIdx.x != 0) return;
+  double s = 0, c = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    neumaier(s, c, part[2 * b]);
+    c += part[2 * b + 1];
+  }
+  *out = s + c;
+}
+
+int norm2_blocks(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>((n + kNormThreads - 1) / kNormThreads, 1), 1024); }
+
+cudaError_t launch_norm2(int dt, const void* X, int64_t n, double* part, double* out, cudaStream_t stream) {
+  const int nb = norm2_blocks(n);
+  if (dt == PQ_C128)
+    k_norm2<double2><<<nb, kNormThreads, 0, stream>>>((const double2*)X, n, part);
+  else
+    k_norm2<float2><<<nb, kNormThreads, 0, stream>>>((const float2*)X, n, part);
+  k_norm2_fold<<<1, 32, 0, stream>>>(part, nb, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_slice_sum(int dt, const void* X, int64_t n, int64_t nb, double* acc, double* comp,
