@@ -56,7 +56,10 @@
 //                  bf16) per K tile into three TN-column accumulators (levels
 //                  0, 1, 2-4); narrow tiles (TN <= 64) alternate between two
 //                  such sets, so a tile's MMAs do not wait for the epilogue
-//                  of the one before;
+//                  of the one before; 16-wide tiles issue one MMA per A slice
+//                  i against B's slices 0 .. 4-i side by side (N = 16 (5-i),
+//                  10 MMAs per K tile), each slice pair into its own exact
+//                  16-column region;
 //     warps 2-9    A converters: gather A's 64 x 16 complex values of the K
 //                  tile through its index map straight from HBM (the group's
 //                  next K tile in flight while this one is sliced), slice
