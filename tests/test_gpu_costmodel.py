@@ -164,7 +164,8 @@ def test_learned_plan_gains_over_flop_plan(pq, O):
     draw first, while the flop-count planner (the judge and fallback) picks
     the reference's full-wavefunction order with fewer multiply-adds.  Both
     plans run as CUDA graphs, timed interleaved; the learned pick must not be
-    slower (it ran 1.14x faster when the model was trained), and both give
+    slower (it ran 1.14x faster when the model was trained, 1.64x with the
+    grouped small-step launches), and both give
     the oracle's state."""
     from pqgb300 import costmodel as CM
     from pqgb300.train_costmodel import time_plan
